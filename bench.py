@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark: batched collectives of the device MPI runtime on one GB300.
+
+Workload (the batched-collectives configuration): 16 communicators of
+4, 8, 12, 16, 24, 32, 40, 48, 56, 64, 72, 80, 88, 96, 128 and 256 ranks
+(1024 rank blocks), each running Bcast, Allreduce(SUM) and Alltoall on int32
+data uniform in [-2^20, 2^20) and FP64 data uniform in [-1, 1), 2^20
+elements per rank (Alltoall: 2^20 / P elements to each peer).
+
+One step = all 96 collective calls.  `value` is algorithmic GB/s of the
+batched form (one persistent cooperative launch, replayed as a CUDA graph),
+with the inputs resident in HBM; algorithmic bytes per call: Bcast P*b,
+Allreduce 2*P*n*s, Alltoall 2*P^2*m.  The plain form (one launch per call and
+communicator) runs the same schedules on the same buffers for comparison.
+`e2e` times the host-buffer entry point (host->device copies of every send
+buffer, the batched plan, device->host copies of every result) on a smaller
+per-rank count stated in the line.  `cpu_baseline` / `--impl reference` run
+the same collectives as an MPI program on the host cores through the hostmpi
+oracle (one process per rank).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "dphpc-project_gb300")
+sys.path.insert(0, PKG)
+
+COMM_SIZES = [4, 8, 12, 16, 24, 32, 40, 48, 56, 64, 72, 80, 88, 96, 128, 256]
+WORKLOAD = ("batched collectives: 16 communicators (4..256 ranks, 1024 rank blocks), "
+            "Bcast + Allreduce(SUM) + Alltoall, int32 and fp64")
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for i, n in enumerate(names):
+                if f[4 + i].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def alg_bytes(sizes, n):
+    total = 0
+    for p in sizes:
+        for s in (4, 8):
+            total += p * n * s              # Bcast
+            total += 2 * p * n * s          # Allreduce
+            per = n // p
+            total += 2 * p * p * per * s    # Alltoall
+    return total
+
+
+def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1):
+    """Device buffers (one tensor per communicator and role) and descriptors."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    dev = torch.device("cuda")
+    comms, keep, descs, bufs = [], [], [], []
+    for p in sizes:
+        c = coll.Comm(lib, p)
+        comms.append(c)
+        per = n // p
+        for dt, tdt in (("int32", torch.int32), ("float64", torch.float64)):
+            es = 4 if dt == "int32" else 8
+            def rnd(count):
+                if dt == "int32":
+                    return torch.randint(-(1 << 20), 1 << 20, (count,), dtype=tdt, device=dev, generator=g)
+                return torch.rand(count, dtype=tdt, device=dev, generator=g) * 2 - 1
+            bc = rnd(p * n)
+            ar_in, ar_out = rnd(p * n), torch.empty(p * n, dtype=tdt, device=dev)
+            a2_in, a2_out = rnd(p * per * p), torch.empty(p * per * p, dtype=tdt, device=dev)
+            bufs += [bc, ar_in, ar_out, a2_in, a2_out]
+            ptr = lambda t, stride: [t.data_ptr() + r * stride * es for r in range(p)]
+            descs.append(coll.make_desc(c, coll.COLL_BCAST, dt, n, None, ptr(bc, n), 0, 0, keep))
+            descs.append(coll.make_desc(c, coll.COLL_ALLREDUCE, dt, n, ptr(ar_in, n), ptr(ar_out, n),
+                                        coll.OP_SUM, 0, keep))
+            descs.append(coll.make_desc(c, coll.COLL_ALLTOALL, dt, per, ptr(a2_in, per * p),
+                                        ptr(a2_out, per * p), 0, 0, keep))
+    plan = coll.Plan(lib, descs, threads=threads, batched=batched)
+    return plan, comms, keep, bufs, descs
+
+
+def time_plan(torch, plan, steps, warmup, stream):
+    for _ in range(warmup):
+        plan.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        plan.launch(stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0
+
+
+def run_oracle_bench(lg: int, iters: int, ranks: int = 1024, timeout: float = 900):
+    exe = os.path.join(ROOT, "oracle", "build", "bin", "coll_bench")
+    if not os.path.exists(exe):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), f"-j{os.cpu_count()}"], check=True,
+                       capture_output=True)
+    r = subprocess.run([exe, str(lg), str(iters), "---gpumpi", "-n", str(ranks)], capture_output=True,
+                       text=True, timeout=timeout)
+    m = re.search(r"coll_bench time ([0-9.]+) s bytes ([0-9.]+) GBps ([0-9.]+)", r.stdout)
+    if r.returncode != 0 or not m:
+        raise RuntimeError(f"oracle benchmark failed: {r.stdout[-500:]} {r.stderr[-500:]}")
+    return float(m.group(3)), float(m.group(1)), float(m.group(2))
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    lg, iters = args.cpu_lg, args.cpu_iters
+    vals = []
+    for _ in range(args.warmup):
+        run_oracle_bench(lg, 1)
+    t0 = time.time()
+    for _ in range(args.steps):
+        gbps, secs, nbytes = run_oracle_bench(lg, iters)
+        vals.append(gbps)
+    wall = time.time() - t0
+    value = sum(vals) / len(vals)
+    cores = os.cpu_count()
+    sample = (f"1024 host processes (hostmpi), the same 16 communicators and six collectives, "
+              f"2^{lg} elements per rank, {iters} iteration(s) per step")
+    line = {
+        "impl": "reference", "metric": "collective GB/s (batched collectives, algorithmic bytes)",
+        "value": round(value, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * wall / max(1, args.steps), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "elements_per_rank": 1 << lg, "comm_sizes": COMM_SIZES,
+                   "l2": "inputs larger than L2 not applicable (host memory)"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--lg", type=int, default=20, help="log2 elements per rank")
+    ap.add_argument("--threads", type=int, default=128)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--e2e-lg", type=int, default=16)
+    ap.add_argument("--cpu-lg", type=int, default=16)
+    ap.add_argument("--cpu-iters", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+    import gpumpi_coll as coll
+    import gpumpi_host as host
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")   # replicas only: used for the barrier and max-over-ranks
+
+    lib = coll.bind(host.load_library())
+    n = 1 << args.lg
+    stream = torch.cuda.Stream()
+    peak, peak_kind = load_peaks()
+
+    # batched form, graph-captured
+    plan, comms, keep, bufs, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, args.threads)
+    plan.capture(stream.cuda_stream)
+    launches0 = lib.gpumpi_kernel_launches()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            plan.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        secs = time_plan(torch, plan, args.steps, 0, stream)
+    launches = lib.gpumpi_kernel_launches() - launches0 - args.warmup
+    err = coll.status(lib)
+    if err:
+        raise SystemExit(f"device error during benchmark: {err}")
+    if dist:
+        t = torch.tensor([secs], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+    nbytes = alg_bytes(COMM_SIZES, n)
+    per_step = secs / args.steps
+    value = nbytes * args.steps * world / secs / 1e9
+    kernel_gbs = nbytes / per_step / 1e9
+
+    # plain form on the same buffers
+    plain = coll.Plan(lib, descs, threads=args.threads, batched=False)
+    psecs = time_plan(torch, plain, args.plain_steps, 1, stream)
+    plain_gbs = nbytes * args.plain_steps / psecs / 1e9
+    plain.close()
+    plan.close()
+    del bufs
+    torch.cuda.empty_cache()
+
+    # end to end through the host-buffer entry point (smaller per-rank count)
+    ne = 1 << args.e2e_lg
+    eplan, ecomms, ekeep, ebufs, edescs = build_plan(coll, lib, torch, COMM_SIZES, ne, True, args.threads,
+                                                     seed=2)
+    sizes_by_comm = {c.h.value: c.n for c in ecomms}
+    layout = []
+    for d in edescs:
+        p = sizes_by_comm[d.comm]
+        es = 4 if d.dtype == coll.DT["int32"] else 8
+        nin = {coll.COLL_BCAST: d.count, coll.COLL_ALLREDUCE: d.count, coll.COLL_ALLTOALL: d.count * p}[d.op]
+        layout += [nin * es] * p
+    total = sum(layout)
+    hsend = torch.empty(total, dtype=torch.uint8).pin_memory()
+    hrecv = torch.empty(total, dtype=torch.uint8).pin_memory()
+    hsend.random_(0, 255)
+    hs, hr, off = [], [], 0
+    for nb in layout:
+        hs.append(hsend.data_ptr() + off)
+        hr.append(hrecv.data_ptr() + off)
+        off += nb
+    ebytes = alg_bytes(COMM_SIZES, ne)
+    for _ in range(2):
+        eplan.run_host(hs, hr, stream.cuda_stream)
+    torch.cuda.synchronize()
+    e_steps = 3
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    for _ in range(e_steps):
+        h2d, d2h = eplan.run_host(hs, hr, stream.cuda_stream)
+        stream.synchronize()
+    esecs = time.perf_counter() - t0
+    e2e_gbs = ebytes * e_steps / esecs / 1e9
+    eplan.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cgbps, csecs, cbytes = run_oracle_bench(args.cpu_lg, args.cpu_iters)
+            cpu = {"value": round(cgbps, 3), "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": (f"hostmpi, 1024 processes, same communicators and collectives, 2^{args.cpu_lg} "
+                              f"elements per rank, {args.cpu_iters} iterations ({csecs:.2f} s timed)")}
+        except Exception as e:  # reported, not fatal
+            cpu = {"value": None, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": "collective GB/s (batched collectives, algorithmic bytes)",
+            "value": round(value, 2),
+            "unit": "GB/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(per_step * 1000, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "int32+f64",
+            "data": "synthetic (seeded uniform int32 [-2^20,2^20), fp64 [-1,1))",
+            "config": {"workload": WORKLOAD, "elements_per_rank": n, "comm_sizes": COMM_SIZES,
+                       "threads_per_rank": args.threads, "form": "batched, CUDA graph replay",
+                       "l2": "inputs larger than L2 (each step touches ~%.0f GB)" % (nbytes / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plain": {"value": round(plain_gbs, 2), "unit": "GB/s", "launches_per_step": len(descs),
+                      "batched_over_plain": round(value / world / plain_gbs, 2)},
+            "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind, "traffic": None},
+            "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    for c in comms + ecomms:
+        c.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,562 @@
+// Host-driven collectives: communicators whose ranks are thread blocks, and
+// plans that run a list of collective calls either as one kernel launch per
+// call ("plain") or as one persistent cooperative launch in which the blocks
+// of every communicator run their communicator's calls in order ("batched").
+// Both forms execute the same device schedules as the MPI_* calls of
+// converted programs (coll.cu), so their results are identical and their
+// speed differs only by launch structure.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <vector>
+
+#include "gpumpi.h"
+#include "hostjob.h"
+#include "rt.cuh"
+
+extern __device__ MPI_Op_impl gm_builtin_ops[GPUMPI_NUM_BUILTIN_OPS];
+
+namespace gm {
+
+struct DevDesc {
+    int op;
+    int dtype;
+    int redop;
+    int root;
+    u64 count;
+    int comm;       // index into the plan's communicator table
+    int esize;
+    int algo;
+    int pad;
+    void** sbufs;   // [P] device array
+    void** rbufs;   // [P]
+};
+
+struct DevComm {
+    MPI_Comm_impl* handles;   // [P] per-rank handles (sequence numbers persist)
+    int size;
+    int pad;
+};
+
+struct PlanArgs {
+    Job* job;
+    const DevDesc* descs;
+    const int* comm_first;    // [ncomm + 1]: descriptor range of each communicator
+    const int* slot_comm;     // [nslots], nullptr = every block in communicator 0
+    const int* slot_rank;     // [nslots], nullptr = rank is blockIdx.x
+    const DevComm* comms;
+};
+
+static __device__ int run_desc(const DevDesc& d, MPI_Comm_impl* comm, int rank, int tid, int T) {
+    CollArgs a;
+    memset(&a, 0, sizeof(a));
+    a.comm = comm;
+    a.root = d.root;
+    a.algo = d.algo;
+    a.ssize = a.rsize = d.esize;
+    a.dtype = (MPI_Datatype)d.dtype;
+    a.op = &gm_builtin_ops[d.redop];
+    a.opi = d.redop;
+    a.ufn = nullptr;
+    const void* sb = d.sbufs ? ldcg(&d.sbufs[rank]) : nullptr;
+    void* rb = d.rbufs ? ldcg(&d.rbufs[rank]) : nullptr;
+    switch (d.op) {
+        case GPUMPI_COLL_BARRIER: return coll_barrier(comm, tid, T);
+        case GPUMPI_COLL_BCAST:
+            a.rbuf = rb;
+            a.count = d.count * d.esize;
+            return coll_bcast(a, tid, T);
+        case GPUMPI_COLL_REDUCE:
+            a.sbuf = sb;
+            a.rbuf = rb;
+            a.count = d.count;
+            return coll_reduce(a, tid, T);
+        case GPUMPI_COLL_ALLREDUCE:
+            a.sbuf = sb;
+            a.rbuf = rb;
+            a.count = d.count;
+            return coll_allreduce(a, tid, T);
+        case GPUMPI_COLL_ALLTOALL:
+            a.sbuf = sb;
+            a.rbuf = rb;
+            a.a0 = (long long)d.count;
+            a.a1 = (long long)d.count;
+            return coll_alltoallv(a, tid, T);
+        case GPUMPI_COLL_ALLGATHER:
+            a.sbuf = sb;
+            a.rbuf = rb;
+            a.a0 = (long long)d.count;
+            a.a1 = (long long)d.count;
+            return coll_allgatherv(a, tid, T);
+        default: return MPI_ERR_ARG;
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(1024) gpumpi_plan_kernel(PlanArgs A) {
+    BlockCtx& b = bctx();
+    const int slot = blockIdx.x;
+    const int c = A.slot_comm ? A.slot_comm[slot] : 0;
+    const int rank = A.slot_rank ? A.slot_rank[slot] : slot;
+    if (threadIdx.x == 0) {
+        b.job = A.job;
+        b.priv = nullptr;
+        b.rank = rank;
+        b.slot = slot;
+        b.T = (int)blockDim.x;
+        b.leader_mode = 0;
+        b.in_call = 0;
+    }
+    __syncthreads();
+    MPI_Comm_impl* comm = &A.comms[c].handles[rank];
+    const int tid = (int)threadIdx.x, T = (int)blockDim.x;
+    for (int i = A.comm_first[c]; i < A.comm_first[c + 1]; i++) {
+        if (run_desc(A.descs[i], comm, rank, tid, T) != MPI_SUCCESS) break;
+    }
+}
+
+}  // namespace gm
+
+using namespace gm;
+
+// ------------------------------------------------------------------ host side
+struct gpumpi_comm_s {
+    int n;
+    char* base;          // device allocation
+    DevComm* dcomm;      // device DevComm
+    DevComm hcomm;
+};
+
+struct gpumpi_plan_s {
+    int ndesc;
+    int ncomm;
+    int batched;
+    int threads;
+    size_t smem;
+    char* base;                       // device allocation
+    PlanArgs batch_args;              // batched launch
+    std::vector<PlanArgs> plain_args; // one per descriptor
+    std::vector<int> plain_grid;
+    int total_slots;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<gpumpi_coll_desc> descs;   // host copies for the host-buffer path
+    std::vector<std::vector<void*>> sb, rb;
+};
+
+namespace {
+
+std::atomic<unsigned long long> g_launches{0};
+
+struct ApiJob {
+    Job* djob = nullptr;
+    int* status = nullptr;
+    char* err = nullptr;
+};
+ApiJob g_api;
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            char m_[300];                                                                 \
+            snprintf(m_, sizeof(m_), "%s: %s", #call, cudaGetErrorString(e_));            \
+            set_last_error(m_);                                                           \
+            return GPUMPI_ECUDA;                                                          \
+        }                                                                                 \
+    } while (0)
+
+int api_job() {
+    if (g_api.djob) return GPUMPI_OK;
+    Job hj;
+    memset(&hj, 0, sizeof(hj));
+    char* mem = nullptr;
+    CK(cudaMalloc(&mem, sizeof(Job) + 64 + 256));
+    CK(cudaMemset(mem, 0, sizeof(Job) + 64 + 256));
+    hj.id = -1;
+    hj.timeout_ns = 30ull * 1000000000ull;
+    hj.status = (int*)(mem + sizeof(Job));
+    hj.err_msg = mem + sizeof(Job) + 64;
+    CK(cudaMemcpy(mem, &hj, sizeof(Job), cudaMemcpyHostToDevice));
+    g_api.djob = (Job*)mem;
+    g_api.status = hj.status;
+    g_api.err = hj.err_msg;
+    return GPUMPI_OK;
+}
+
+int esize_of(int dtype) {
+    switch (dtype) {
+        case MPI_CHAR: case MPI_SIGNED_CHAR: case MPI_UNSIGNED_CHAR: case MPI_BYTE: case MPI_INT8_T:
+        case MPI_UINT8_T: case MPI_C_BOOL: return 1;
+        case MPI_SHORT: case MPI_UNSIGNED_SHORT: case MPI_INT16_T: case MPI_UINT16_T: return 2;
+        case MPI_INT: case MPI_UNSIGNED: case MPI_FLOAT: case MPI_INT32_T: case MPI_UINT32_T: return 4;
+        case MPI_LONG: case MPI_LONG_LONG_INT: case MPI_LONG_LONG: case MPI_UNSIGNED_LONG:
+        case MPI_UNSIGNED_LONG_LONG: case MPI_DOUBLE: case MPI_INT64_T: case MPI_UINT64_T: return 8;
+        default: return -1;
+    }
+}
+
+// Bytes a rank sends / receives for a descriptor.
+void desc_bytes(const gpumpi_coll_desc& d, int P, size_t* in, size_t* out) {
+    size_t e = (size_t)esize_of(d.dtype) * d.count;
+    switch (d.op) {
+        case GPUMPI_COLL_BCAST: *in = e; *out = e; break;
+        case GPUMPI_COLL_REDUCE:
+        case GPUMPI_COLL_ALLREDUCE: *in = e; *out = e; break;
+        case GPUMPI_COLL_ALLTOALL: *in = e * P; *out = e * P; break;
+        case GPUMPI_COLL_ALLGATHER: *in = e; *out = e * P; break;
+        default: *in = *out = 0;
+    }
+}
+
+int launch(const void* kern, int grid, int threads, size_t smem, PlanArgs* args, cudaStream_t st) {
+    void* params[] = {args};
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelExC(&cfg, kern, params));
+    g_launches++;
+    return GPUMPI_OK;
+}
+
+}  // namespace
+
+extern "C" int gpumpi_comm_create(int nranks, gpumpi_comm_t* out) {
+    if (nranks <= 0 || !out) return GPUMPI_EINVAL;
+    int rc = api_job();
+    if (rc) return rc;
+    const size_t n = (size_t)nranks;
+    size_t off_cs = 0;
+    size_t off_pub = 256;
+    size_t off_flags = off_pub + ((sizeof(Pub) * n + 255) & ~(size_t)255);
+    size_t off_h = off_flags + ((3 * sizeof(u64) * n + 255) & ~(size_t)255);
+    size_t off_dc = off_h + ((sizeof(MPI_Comm_impl) * n + 255) & ~(size_t)255);
+    size_t total = off_dc + 256;
+    char* base = nullptr;
+    CK(cudaMalloc(&base, total));
+    CK(cudaMemset(base, 0, total));
+    CommShared cs;
+    memset(&cs, 0, sizeof(cs));
+    cs.size = nranks;
+    cs.ctx = 1;
+    cs.members = nullptr;
+    cs.pub = (Pub*)(base + off_pub);
+    cs.arrive = (u64*)(base + off_flags);
+    cs.mid = cs.arrive + n;
+    cs.depart = cs.arrive + 2 * n;
+    CK(cudaMemcpy(base + off_cs, &cs, sizeof(cs), cudaMemcpyHostToDevice));
+    std::vector<MPI_Comm_impl> h(n);
+    for (int r = 0; r < nranks; r++) {
+        h[r].kind = 1;
+        h[r].ctx = 1;
+        h[r].size = nranks;
+        h[r].rank = r;
+        h[r].refcnt = 1;
+        h[r].pad = 0;
+        h[r].cs = (CommShared*)(base + off_cs);
+        h[r].seq = 0;
+    }
+    CK(cudaMemcpy(base + off_h, h.data(), sizeof(MPI_Comm_impl) * n, cudaMemcpyHostToDevice));
+    gpumpi_comm_s* c = new gpumpi_comm_s();
+    c->n = nranks;
+    c->base = base;
+    c->hcomm.handles = (MPI_Comm_impl*)(base + off_h);
+    c->hcomm.size = nranks;
+    c->hcomm.pad = 0;
+    c->dcomm = (DevComm*)(base + off_dc);
+    CK(cudaMemcpy(c->dcomm, &c->hcomm, sizeof(DevComm), cudaMemcpyHostToDevice));
+    *out = c;
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_comm_destroy(gpumpi_comm_t c) {
+    if (!c) return GPUMPI_EINVAL;
+    cudaFree(c->base);
+    delete c;
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_comm_size(gpumpi_comm_t c, int* n) {
+    if (!c || !n) return GPUMPI_EINVAL;
+    *n = c->n;
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int threads, int batched,
+                                  gpumpi_plan_t* out) {
+    if (!descs || ndesc <= 0 || !out) return GPUMPI_EINVAL;
+    if (threads == 0) threads = 128;
+    if (threads < 64 || threads > 1024 || threads % 32) return GPUMPI_EINVAL;
+    int rc = api_job();
+    if (rc) return rc;
+    // communicators in order of first use; descriptors grouped by communicator, order kept
+    std::vector<gpumpi_comm_t> comms;
+    std::vector<int> cidx(ndesc);
+    for (int i = 0; i < ndesc; i++) {
+        const gpumpi_coll_desc& d = descs[i];
+        if (!d.comm || esize_of(d.dtype) < 0 || d.op < 0 || d.op > GPUMPI_COLL_ALLGATHER) return GPUMPI_EINVAL;
+        if ((d.op == GPUMPI_COLL_REDUCE || d.op == GPUMPI_COLL_ALLREDUCE) && (d.redop < 0 || d.redop > 3))
+            return GPUMPI_EINVAL;
+        if ((d.op == GPUMPI_COLL_BCAST || d.op == GPUMPI_COLL_REDUCE) && (d.root < 0 || d.root >= d.comm->n))
+            return GPUMPI_EINVAL;
+        auto it = std::find(comms.begin(), comms.end(), d.comm);
+        cidx[i] = (int)(it - comms.begin());
+        if (it == comms.end()) comms.push_back(d.comm);
+    }
+    const int ncomm = (int)comms.size();
+    std::vector<int> order(ndesc);
+    for (int i = 0; i < ndesc; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cidx[a] < cidx[b]; });
+    std::vector<int> comm_first(ncomm + 1, 0);
+    for (int i = 0; i < ndesc; i++) comm_first[cidx[i] + 1]++;
+    for (int c = 0; c < ncomm; c++) comm_first[c + 1] += comm_first[c];
+    int total_slots = 0;
+    for (auto* c : comms) total_slots += c->n;
+    size_t ptrs = 0;
+    for (int i = 0; i < ndesc; i++) ptrs += 2 * (size_t)descs[i].comm->n;
+    // device layout: descs | comm_first | slot_comm | slot_rank | comms | per-desc comm_first pairs | pointers
+    size_t off_desc = 0;
+    size_t off_cf = off_desc + sizeof(DevDesc) * ndesc;
+    size_t off_sc = (off_cf + sizeof(int) * (ncomm + 1) + 15) & ~(size_t)15;
+    size_t off_sr = off_sc + sizeof(int) * total_slots;
+    size_t off_cm = (off_sr + sizeof(int) * total_slots + 15) & ~(size_t)15;
+    size_t off_pp = off_cm + sizeof(DevComm) * ncomm;
+    size_t off_pc = (off_pp + sizeof(int) * 2 * ndesc + 15) & ~(size_t)15;
+    size_t off_ptr = off_pc + sizeof(DevComm) * ndesc;
+    size_t total = off_ptr + sizeof(void*) * ptrs + 16;
+    gpumpi_plan_s* p = new gpumpi_plan_s();
+    CK(cudaMalloc(&p->base, total));
+    char* base = p->base;
+    std::vector<char> h(total, 0);
+    DevDesc* hd = (DevDesc*)(h.data() + off_desc);
+    void** hp = (void**)(h.data() + off_ptr);
+    size_t pk = 0;
+    p->descs.assign(descs, descs + ndesc);
+    p->sb.resize(ndesc);
+    p->rb.resize(ndesc);
+    for (int k = 0; k < ndesc; k++) {
+        const int i = order[k];
+        const gpumpi_coll_desc& d = descs[i];
+        const int P = d.comm->n;
+        DevDesc& x = hd[k];
+        x.op = d.op;
+        x.dtype = d.dtype;
+        x.redop = d.redop;
+        x.root = d.root;
+        x.count = d.count;
+        x.comm = cidx[i];
+        x.esize = esize_of(d.dtype);
+        x.algo = 0;
+        x.sbufs = (void**)(base + off_ptr + sizeof(void*) * pk);
+        for (int r = 0; r < P; r++) hp[pk++] = d.sendbufs ? d.sendbufs[r] : nullptr;
+        x.rbufs = (void**)(base + off_ptr + sizeof(void*) * pk);
+        for (int r = 0; r < P; r++) hp[pk++] = d.recvbufs ? d.recvbufs[r] : nullptr;
+        p->sb[i].assign(hp + pk - 2 * P, hp + pk - P);
+        p->rb[i].assign(hp + pk - P, hp + pk);
+    }
+    memcpy(h.data() + off_cf, comm_first.data(), sizeof(int) * (ncomm + 1));
+    int* sc = (int*)(h.data() + off_sc);
+    int* sr = (int*)(h.data() + off_sr);
+    int s = 0;
+    for (int c = 0; c < ncomm; c++)
+        for (int r = 0; r < comms[c]->n; r++) {
+            sc[s] = c;
+            sr[s] = r;
+            s++;
+        }
+    DevComm* hc = (DevComm*)(h.data() + off_cm);
+    for (int c = 0; c < ncomm; c++) hc[c] = comms[c]->hcomm;
+    // plain launches: each descriptor alone, its own communicator at index 0
+    int* pp = (int*)(h.data() + off_pp);
+    DevComm* pc = (DevComm*)(h.data() + off_pc);
+    for (int k = 0; k < ndesc; k++) {
+        pp[2 * k] = 0;
+        pp[2 * k + 1] = 1;
+        pc[k] = comms[hd[k].comm]->hcomm;
+    }
+    CK(cudaMemcpy(base, h.data(), total, cudaMemcpyHostToDevice));
+    p->ndesc = ndesc;
+    p->ncomm = ncomm;
+    p->batched = batched;
+    p->threads = threads;
+    p->smem = sizeof(BlockCtx) + 64;
+    p->total_slots = total_slots;
+    p->batch_args.job = g_api.djob;
+    p->batch_args.descs = (const DevDesc*)(base + off_desc);
+    p->batch_args.comm_first = (const int*)(base + off_cf);
+    p->batch_args.slot_comm = (const int*)(base + off_sc);
+    p->batch_args.slot_rank = (const int*)(base + off_sr);
+    p->batch_args.comms = (const DevComm*)(base + off_cm);
+    p->plain_args.resize(ndesc);
+    p->plain_grid.resize(ndesc);
+    for (int k = 0; k < ndesc; k++) {
+        PlanArgs& a = p->plain_args[k];
+        a.job = g_api.djob;
+        a.descs = (const DevDesc*)(base + off_desc) + k;
+        a.comm_first = (const int*)(base + off_pp) + 2 * k;
+        a.slot_comm = nullptr;
+        a.slot_rank = nullptr;
+        a.comms = (const DevComm*)(base + off_pc) + k;
+        p->plain_grid[k] = comms[hd[k].comm]->n;
+    }
+    // co-residency: every rank block of one launch must fit on the GPU at once
+    int per = 0, sms = 0, dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)gpumpi_plan_kernel, threads, p->smem));
+    int need = batched ? total_slots : *std::max_element(p->plain_grid.begin(), p->plain_grid.end());
+    if ((long long)per * sms < need) {
+        char m[200];
+        snprintf(m, sizeof(m), "%d rank blocks of %d threads cannot be co-resident (max %d)", need, threads,
+                 per * sms);
+        set_last_error(m);
+        cudaFree(p->base);
+        delete p;
+        return GPUMPI_ENORES;
+    }
+    *out = p;
+    return GPUMPI_OK;
+}
+
+static int plan_enqueue(gpumpi_plan_t p, cudaStream_t st) {
+    const void* k = (const void*)gpumpi_plan_kernel;
+    if (p->batched) return launch(k, p->total_slots, p->threads, p->smem, &p->batch_args, st);
+    for (int i = 0; i < p->ndesc; i++) {
+        int rc = launch(k, p->plain_grid[i], p->threads, p->smem, &p->plain_args[i], st);
+        if (rc) return rc;
+    }
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_plan_launch(gpumpi_plan_t p, void* stream) {
+    if (!p) return GPUMPI_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (p->exec) {
+        CK(cudaGraphLaunch(p->exec, st));
+        g_launches += p->batched ? 1 : p->ndesc;
+        return GPUMPI_OK;
+    }
+    return plan_enqueue(p, st);
+}
+
+extern "C" int gpumpi_plan_capture(gpumpi_plan_t p, void* stream) {
+    if (!p) return GPUMPI_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    unsigned long long before = g_launches;
+    int rc = plan_enqueue(p, cap);
+    g_launches = before;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    CK(e);
+    CK(cudaGraphInstantiate(&p->exec, g, 0));
+    p->graph = g;
+    (void)st;
+    return GPUMPI_OK;
+}
+
+// Host-buffer path: copy every rank's send data from host memory, run the
+// plan, copy every rank's result back.  host_send/host_recv hold, for each
+// descriptor in the order given to gpumpi_plan_create, one host pointer per
+// rank (nullptr = skip).
+extern "C" int gpumpi_plan_run_host(gpumpi_plan_t p, void* const* host_send, void* const* host_recv,
+                                    void* stream, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
+    if (!p) return GPUMPI_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t k = 0, bi = 0, bo = 0;
+    for (int d = 0; d < p->ndesc; d++) {
+        const int P = p->descs[d].comm->n;
+        size_t in, out;
+        desc_bytes(p->descs[d], P, &in, &out);
+        for (int r = 0; r < P; r++, k++) {
+            const bool is_bcast = p->descs[d].op == GPUMPI_COLL_BCAST;
+            void* dst = is_bcast ? p->rb[d][r] : p->sb[d][r];
+            if (is_bcast && r != p->descs[d].root) continue;
+            if (host_send && host_send[k] && dst && in) {
+                CK(cudaMemcpyAsync(dst, host_send[k], in, cudaMemcpyHostToDevice, st));
+                bi += in;
+            }
+        }
+    }
+    int rc = gpumpi_plan_launch(p, stream);
+    if (rc) return rc;
+    k = 0;
+    for (int d = 0; d < p->ndesc; d++) {
+        const int P = p->descs[d].comm->n;
+        size_t in, out;
+        desc_bytes(p->descs[d], P, &in, &out);
+        for (int r = 0; r < P; r++, k++) {
+            if (p->descs[d].op == GPUMPI_COLL_REDUCE && r != p->descs[d].root) continue;
+            if (host_recv && host_recv[k] && p->rb[d][r] && out) {
+                CK(cudaMemcpyAsync(host_recv[k], p->rb[d][r], out, cudaMemcpyDeviceToHost, st));
+                bo += out;
+            }
+        }
+    }
+    if (h2d_bytes) *h2d_bytes = bi;
+    if (d2h_bytes) *d2h_bytes = bo;
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_plan_destroy(gpumpi_plan_t p) {
+    if (!p) return GPUMPI_EINVAL;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    cudaFree(p->base);
+    delete p;
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_api_status(char* msg, int len);
+static int one_shot(const gpumpi_coll_desc* descs, int ndesc, int threads, void* stream, int batched) {
+    gpumpi_plan_t p = nullptr;
+    int rc = gpumpi_plan_create(descs, ndesc, threads, batched, &p);
+    if (rc) return rc;
+    rc = gpumpi_plan_launch(p, stream);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    gpumpi_plan_destroy(p);
+    if (rc) return rc;
+    if (e != cudaSuccess) return GPUMPI_ECUDA;
+    return gpumpi_api_status(nullptr, 0);
+}
+
+extern "C" int gpumpi_coll_plain(const gpumpi_coll_desc* descs, int ndesc, int threads, void* stream) {
+    return one_shot(descs, ndesc, threads, stream, 0);
+}
+
+extern "C" int gpumpi_coll_batched(const gpumpi_coll_desc* descs, int ndesc, int threads, void* stream) {
+    return one_shot(descs, ndesc, threads, stream, 1);
+}
+
+// Error state of the collective API's device job; clears it.
+extern "C" int gpumpi_api_status(char* msg, int len) {
+    if (!g_api.djob) return GPUMPI_OK;
+    int st[16];
+    CK(cudaMemcpy(st, g_api.status, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st[1] == 0) return GPUMPI_OK;
+    char m[256];
+    CK(cudaMemcpy(m, g_api.err, sizeof(m), cudaMemcpyDeviceToHost));
+    m[255] = 0;
+    if (msg && len > 0) snprintf(msg, len, "error %d on rank %d: %s", st[1], st[2], m);
+    char full[320];
+    snprintf(full, sizeof(full), "collective job error %d on rank %d: %s", st[1], st[2], m);
+    set_last_error(full);
+    CK(cudaMemset(g_api.status, 0, sizeof(st)));
+    return GPUMPI_EJOB;
+}
+
+extern "C" uint64_t gpumpi_kernel_launches(void) { return g_launches; }

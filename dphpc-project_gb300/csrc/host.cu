@@ -1,0 +1,473 @@
+// Host side of the program launcher: option parsing compatible with the
+// reference's "---gpumpi" syntax (gpu_libs/gpu_main/main.cu:49-98), job memory
+// layout in HBM, co-residency check (main.cu:189-209, done here with the
+// cooperative-launch occupancy query), launch, output drain and exit status.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+#include <time.h>
+
+#include <string>
+#include <vector>
+
+#include "gpumpi.h"
+#include "hostjob.h"
+#include "rt.cuh"
+
+static_assert(GPUMPI_DT_INT == MPI_INT && GPUMPI_DT_DOUBLE == MPI_DOUBLE && GPUMPI_DT_BYTE == MPI_BYTE &&
+                  GPUMPI_DT_INT64 == MPI_INT64_T && GPUMPI_DT_FLOAT == MPI_FLOAT,
+              "host datatype codes follow the device enum");
+
+extern "C" size_t gpumpi_heap_meta_bytes();
+
+namespace gm {
+
+static char g_last_error[512] = "";
+
+void set_last_error(const char* msg) {
+    snprintf(g_last_error, sizeof(g_last_error), "%s", msg);
+}
+
+#define HCHECK(call)                                                                  \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            char m_[400];                                                             \
+            snprintf(m_, sizeof(m_), "%s failed: %s", #call, cudaGetErrorString(e_)); \
+            set_last_error(m_);                                                       \
+            fprintf(stderr, "GPUMPI: %s\n", m_);                                      \
+            return GPUMPI_ECUDA;                                                      \
+        }                                                                             \
+    } while (0)
+
+// ------------------------------------------------------------------ layout
+struct Carver {
+    size_t off = 0;
+    size_t take(size_t bytes, size_t align = 256) {
+        off = (off + align - 1) & ~(align - 1);
+        size_t o = off;
+        off += bytes;
+        return o;
+    }
+};
+
+void opts_defaults(gpumpi_opts* o) {
+    if (o->stack_bytes == 0) o->stack_bytes = 16 * 1024;
+    if (o->heap_bytes == 0) o->heap_bytes = (size_t)1 << 30;
+    if (o->max_requests == 0) o->max_requests = 1024;
+    if (o->eager_bytes == 0) o->eager_bytes = 4096;
+    if (o->timeout_s <= 0) o->timeout_s = 60.0;
+    if (o->out_bytes == 0) o->out_bytes = (size_t)16 << 20;
+}
+
+size_t job_footprint(const gpumpi_opts& o, int n) {
+    HostJob tmp;
+    return host_job_layout(tmp, o, n, 0, nullptr);
+}
+
+// Compute (and, when base != nullptr, fill) the layout of one job.
+size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, char* base) {
+    Carver c;
+    const size_t eager = (o.eager_bytes + 15) & ~(size_t)15;
+    const u32 npages = (u32)((o.heap_bytes + 65535) / 65536);
+    const size_t meta_bytes = gpumpi_heap_meta_bytes();
+    // zeroed control region first
+    size_t z0 = c.take(0);
+    size_t o_mbox = c.take(sizeof(Mailbox) * (size_t)n, 128);
+    size_t o_wcs = c.take(sizeof(CommShared), 128);
+    size_t o_wpub = c.take(sizeof(Pub) * (size_t)n);
+    size_t o_warr = c.take(sizeof(u64) * (size_t)n * 3);
+    size_t o_scs = c.take(sizeof(CommShared) * (size_t)n, 128);
+    size_t o_spub = c.take(sizeof(Pub) * (size_t)n);
+    size_t o_sarr = c.take(sizeof(u64) * (size_t)n * 3);
+    size_t o_status = c.take(sizeof(int) * 16);
+    size_t o_ret = c.take(sizeof(int) * (size_t)n);
+    size_t o_offs = c.take(sizeof(u64) * 4);
+    size_t o_hctl = c.take(sizeof(u32) * (12 + 12 * 32 + 1 + 8) + sizeof(u64) * 64);
+    size_t o_meta = c.take(meta_bytes * npages);
+    size_t o_arena = c.take(((size_t)4 << 20) + (size_t)n * 4096);
+    size_t arena_bytes = ((size_t)4 << 20) + (size_t)n * 4096;
+    size_t z1 = c.take(0);
+    // not zeroed
+    size_t o_clsp = c.take(sizeof(u32) * 12 * (size_t)npages);
+    size_t o_eager = c.take(eager * MB_SLOTS * (size_t)n);
+    size_t o_priv = c.take(sizeof(RankPriv) * (size_t)n);
+    size_t o_req = c.take(sizeof(MPI_Request_impl) * (size_t)n * o.max_requests);
+    size_t o_stage = c.take((size_t)STAGE_BYTES * n);
+    size_t o_cscr = c.take((size_t)COLL_SCRATCH_BYTES * n);
+    size_t o_out = c.take(o.out_bytes);
+    size_t o_err = c.take(o.out_bytes);
+    size_t o_errmsg = c.take(256);
+    size_t o_heap = c.take((size_t)npages * 65536, 65536);
+    size_t o_job = c.take(sizeof(Job));
+    size_t total = c.take(0);
+    hj.zero_off = z0;
+    hj.zero_bytes = z1 - z0;
+    hj.clsp_off = o_clsp;
+    hj.clsp_bytes = sizeof(u32) * 12 * (size_t)npages;
+    hj.total = total;
+    hj.nranks = n;
+    hj.job_off = o_job;
+    if (!base) return total;
+    hj.base = base;
+    Job& j = hj.job;
+    memset(&j, 0, sizeof(j));
+    j.id = job_id;
+    j.nranks = n;
+    j.threads = o.threads_per_rank;
+    j.max_requests = o.max_requests;
+    j.timeout_ns = (u64)(o.timeout_s * 1e9);
+    j.eager_bytes = eager;
+    j.mbox = (Mailbox*)(base + o_mbox);
+    j.eager = base + o_eager;
+    j.priv = (RankPriv*)(base + o_priv);
+    j.reqpool = (MPI_Request_impl*)(base + o_req);
+    j.stage = base + o_stage;
+    j.coll_scratch = base + o_cscr;
+    j.world_cs = (CommShared*)(base + o_wcs);
+    j.self_cs = (CommShared*)(base + o_scs);
+    j.arena = base + o_arena;
+    j.arena_bytes = arena_bytes;
+    u64* offs = (u64*)(base + o_offs);
+    j.out_off = offs + 0;
+    j.errout_off = offs + 1;
+    j.arena_off = offs + 2;
+    j.out = base + o_out;
+    j.errout = base + o_err;
+    j.out_bytes = o.out_bytes;
+    j.status = (int*)(base + o_status);
+    j.retvals = (int*)(base + o_ret);
+    j.err_msg = base + o_errmsg;
+    // heap
+    Heap& h = j.heap;
+    h.base = base + o_heap;
+    h.bytes = (u64)npages * 65536;
+    h.npages = npages;
+    h.meta = (PageMeta*)(base + o_meta);
+    u32* hc = (u32*)(base + o_hctl);
+    h.cls_count = hc;
+    h.cls_hint = hc + 12;
+    h.next_page = hc + 12 + 12 * 32;
+    h.stats = hc + 12 + 12 * 32 + 1;
+    h.large_free = (u64*)(((uintptr_t)(hc + 12 + 12 * 32 + 1 + 8) + 7) & ~(uintptr_t)7);
+    h.cls_pages = (u32*)(base + o_clsp);
+    // communicator tables (host copies, uploaded by the caller)
+    hj.world.size = n;
+    hj.world.ctx = 1;
+    hj.world.members = nullptr;
+    hj.world.pub = (Pub*)(base + o_wpub);
+    hj.world.arrive = (u64*)(base + o_warr);
+    hj.world.mid = hj.world.arrive + n;
+    hj.world.depart = hj.world.arrive + 2 * (size_t)n;
+    hj.selfs.resize(n);
+    for (int r = 0; r < n; r++) {
+        CommShared& s = hj.selfs[r];
+        memset(&s, 0, sizeof(s));
+        s.size = 1;
+        s.ctx = 2;
+        s.pub = (Pub*)(base + o_spub) + r;
+        s.arrive = (u64*)(base + o_sarr) + 3 * (size_t)r;
+        s.mid = s.arrive + 1;
+        s.depart = s.arrive + 2;
+    }
+    return total;
+}
+
+// Zero the control state and upload the job description.
+int host_job_init(HostJob& hj, cudaStream_t st) {
+    HCHECK(cudaMemsetAsync(hj.base + hj.zero_off, 0, hj.zero_bytes, st));
+    HCHECK(cudaMemsetAsync(hj.base + hj.clsp_off, 0xff, hj.clsp_bytes, st));
+    HCHECK(cudaMemcpyAsync(hj.job.world_cs, &hj.world, sizeof(CommShared), cudaMemcpyHostToDevice, st));
+    HCHECK(cudaMemcpyAsync(hj.job.self_cs, hj.selfs.data(), sizeof(CommShared) * hj.selfs.size(),
+                           cudaMemcpyHostToDevice, st));
+    HCHECK(cudaMemcpyAsync(hj.base + hj.job_off, &hj.job, sizeof(Job), cudaMemcpyHostToDevice, st));
+    return GPUMPI_OK;
+}
+
+// ------------------------------------------------------------------ args
+static bool parse_size(const char* s, size_t* out) {
+    char* e = nullptr;
+    double v = strtod(s, &e);
+    if (e == s || v < 0) return false;
+    if (*e == 'k' || *e == 'K') v *= 1024.0;
+    else if (*e == 'm' || *e == 'M') v *= 1024.0 * 1024.0;
+    else if (*e == 'g' || *e == 'G') v *= 1024.0 * 1024.0 * 1024.0;
+    *out = (size_t)v;
+    return true;
+}
+
+}  // namespace gm
+
+using namespace gm;
+
+extern "C" const char* gpumpi_last_error(void) { return g_last_error; }
+
+extern "C" int gpumpi_parse_args(int argc, char** argv, gpumpi_opts* o) {
+    memset(o, 0, sizeof(*o));
+    int pos = -1;
+    for (int i = 0; i < argc; i++)
+        if (strcmp(argv[i], "---gpumpi") == 0) pos = i;
+    if (pos < 0) return -1;
+    unsigned blocks = 0, threads = 0;
+    for (int i = pos + 1; i < argc; i++) {
+        std::string a = argv[i];
+        std::string val;
+        bool has_val = false;
+        size_t eq = a.find('=');
+        if (a.rfind("--", 0) == 0 && eq != std::string::npos) {
+            val = a.substr(eq + 1);
+            a = a.substr(0, eq);
+            has_val = true;
+        }
+        auto next = [&](std::string* v) -> bool {
+            if (has_val) {
+                *v = val;
+                return true;
+            }
+            if (i + 1 >= argc) return false;
+            *v = argv[++i];
+            return true;
+        };
+        std::string v;
+        if (a == "-h" || a == "--help") {
+            printf(
+                "GPU MPI (GB300) launcher options after ---gpumpi:\n"
+                "  -n, --numProcs N         MPI ranks\n"
+                "  -g, --blocksPerGrid G    with -b: ranks = G*B when -n is absent\n"
+                "  -b, --threadsPerBlock B\n"
+                "  -t, --threads-per-rank T threads in each rank block (default: auto)\n"
+                "  -s, --stackSize BYTES    per-thread stack (default 16K)\n"
+                "  -p, --heapSize BYTES     device heap (default 1G)\n"
+                "  -e, --pendingBufferSize N outstanding requests per rank (default 1024)\n"
+                "  --eager-bytes BYTES      eager/rendezvous threshold (default 4096)\n"
+                "  --timeout-ms MS          bound of every device wait (default 60000)\n"
+                "  --out-bytes BYTES        output buffer per stream (default 16M)\n"
+                "  --max-seconds S          host wall-clock limit (default none)\n"
+                "  -v, --verbose            launch details on stderr\n");
+            exit(0);
+        } else if (a == "-n" || a == "--numProcs") {
+            if (!next(&v)) return -2;
+            o->nranks = atoi(v.c_str());
+        } else if (a == "-g" || a == "--blocksPerGrid") {
+            if (!next(&v)) return -2;
+            blocks = (unsigned)atoi(v.c_str());
+        } else if (a == "-b" || a == "--threadsPerBlock") {
+            if (!next(&v)) return -2;
+            threads = (unsigned)atoi(v.c_str());
+        } else if (a == "-t" || a == "--threads-per-rank") {
+            if (!next(&v)) return -2;
+            o->threads_per_rank = atoi(v.c_str());
+        } else if (a == "-s" || a == "--stackSize") {
+            if (!next(&v) || !parse_size(v.c_str(), &o->stack_bytes)) return -2;
+        } else if (a == "-p" || a == "--heapSize") {
+            if (!next(&v) || !parse_size(v.c_str(), &o->heap_bytes)) return -2;
+        } else if (a == "-e" || a == "--pendingBufferSize") {
+            if (!next(&v)) return -2;
+            o->max_requests = atoi(v.c_str());
+        } else if (a == "--eager-bytes") {
+            if (!next(&v) || !parse_size(v.c_str(), &o->eager_bytes)) return -2;
+        } else if (a == "--timeout-ms") {
+            if (!next(&v)) return -2;
+            o->timeout_s = atof(v.c_str()) / 1000.0;
+        } else if (a == "--out-bytes") {
+            if (!next(&v) || !parse_size(v.c_str(), &o->out_bytes)) return -2;
+        } else if (a == "--max-seconds") {
+            if (!next(&v)) return -2;
+            o->max_seconds = atof(v.c_str());
+        } else if (a == "-v" || a == "--verbose") {
+            o->verbose = 1;
+        } else {
+            fprintf(stderr, "GPUMPI: unknown option '%s'\n", a.c_str());
+            return -2;
+        }
+    }
+    if (o->nranks == 0) {
+        // The reference's -g/-b named blocks and threads of one-thread ranks.
+        if (blocks == 0) blocks = 1;
+        if (threads == 0) threads = 1;
+        o->nranks = (int)(blocks * threads);
+    }
+    return pos;
+}
+
+namespace gm {
+
+static double now_s() {
+    timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + ts.tv_nsec * 1e-9;
+}
+
+// Choose threads per rank: the largest of 256/128/64 that keeps every rank
+// resident, given the kernel's register and shared-memory use.
+int choose_threads(const void* kernel, int n, int requested, size_t smem, int* max_resident) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int cand[] = {256, 128, 64};
+    int best = 0;
+    for (int k = 0; k < 3; k++) {
+        int T = requested ? requested : cand[k];
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem) != cudaSuccess) per = 0;
+        if (max_resident) *max_resident = per * sms;
+        if ((long long)per * sms >= n) {
+            best = T;
+            break;
+        }
+        if (requested) break;
+    }
+    return best;
+}
+
+}  // namespace gm
+
+extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog_argv,
+                                  const gpumpi_opts* in_opts) {
+    gpumpi_opts o = *in_opts;
+    opts_defaults(&o);
+    const int n = o.nranks;
+    if (n <= 0) {
+        set_last_error("number of ranks must be positive");
+        return GPUMPI_EINVAL;
+    }
+    const size_t smem = sizeof(BlockCtx) + 64;
+    int max_res = 0;
+    int T = choose_threads(kernel, n, o.threads_per_rank, smem, &max_res);
+    if (T == 0 || T % 32 || T < 64 || T > 1024) {
+        char m[256];
+        snprintf(m, sizeof(m),
+                 "%d ranks cannot all be resident (at most %d rank blocks of %d threads fit); "
+                 "lower -t or -n",
+                 n, max_res, o.threads_per_rank ? o.threads_per_rank : 64);
+        set_last_error(m);
+        fprintf(stderr, "GPUMPI: %s\n", m);
+        return GPUMPI_ENORES;
+    }
+    o.threads_per_rank = T;
+    HCHECK(cudaDeviceSetLimit(cudaLimitStackSize, o.stack_bytes));
+
+    HostJob hj;
+    size_t total = host_job_layout(hj, o, n, 0, nullptr);
+    char* base = nullptr;
+    HCHECK(cudaMalloc(&base, total));
+    host_job_layout(hj, o, n, 0, base);
+
+    // argv in device memory
+    size_t strbytes = 0;
+    for (int i = 0; i < prog_argc; i++) strbytes += strlen(prog_argv[i]) + 1;
+    std::vector<char> hargs(sizeof(char*) * (prog_argc + 1) + strbytes + 16);
+    char* dargs = nullptr;
+    HCHECK(cudaMalloc(&dargs, hargs.size()));
+    {
+        char** ptrs = (char**)hargs.data();
+        char* s = hargs.data() + sizeof(char*) * (prog_argc + 1);
+        for (int i = 0; i < prog_argc; i++) {
+            size_t l = strlen(prog_argv[i]) + 1;
+            memcpy(s, prog_argv[i], l);
+            ptrs[i] = dargs + (s - hargs.data());
+            s += l;
+        }
+        ptrs[prog_argc] = nullptr;
+    }
+    hj.job.argc = prog_argc;
+    hj.job.argv = (char**)dargs;
+    hj.job.threads = T;
+
+    // one job, one slot per rank
+    std::vector<int> slots(2 * (size_t)n);
+    for (int r = 0; r < n; r++) {
+        slots[r] = 0;
+        slots[n + r] = r;
+    }
+    int* dslots = nullptr;
+    HCHECK(cudaMalloc(&dslots, sizeof(int) * 2 * (size_t)n));
+
+    cudaStream_t st;
+    HCHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    HCHECK(cudaMemcpyAsync(dargs, hargs.data(), hargs.size(), cudaMemcpyHostToDevice, st));
+    HCHECK(cudaMemcpyAsync(dslots, slots.data(), sizeof(int) * 2 * (size_t)n, cudaMemcpyHostToDevice, st));
+    int rc = host_job_init(hj, st);
+    if (rc) return rc;
+
+    Launch L;
+    L.jobs = (Job*)(base + hj.job_off);
+    L.njobs = 1;
+    L.nslots = n;
+    L.slot_job = dslots;
+    L.slot_rank = dslots + n;
+    void* args[] = {&L};
+    if (o.verbose)
+        fprintf(stderr, "GPUMPI: %d ranks x %d threads, job memory %.1f MiB, heap %.1f MiB\n", n, T,
+                total / 1048576.0, o.heap_bytes / 1048576.0);
+    const double t0 = now_s();
+    HCHECK(cudaLaunchCooperativeKernel(kernel, dim3(n), dim3(T), args, smem, st));
+    cudaEvent_t done;
+    HCHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    HCHECK(cudaEventRecord(done, st));
+    for (;;) {
+        cudaError_t q = cudaEventQuery(done);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) {
+            HCHECK(q);
+        }
+        if (o.max_seconds > 0 && now_s() - t0 > o.max_seconds) {
+            fprintf(stderr, "GPUMPI: wall-clock limit of %.1f s exceeded; ending the process\n",
+                    o.max_seconds);
+            fflush(stderr);
+            _exit(3);
+        }
+        usleep(200);
+    }
+    HCHECK(cudaStreamSynchronize(st));
+
+    // results
+    Job& j = hj.job;
+    int status[16];
+    u64 offs[4];
+    std::vector<int> rets(n);
+    char errmsg[256];
+    HCHECK(cudaMemcpy(status, j.status, sizeof(status), cudaMemcpyDeviceToHost));
+    HCHECK(cudaMemcpy(offs, j.out_off, sizeof(offs), cudaMemcpyDeviceToHost));
+    HCHECK(cudaMemcpy(rets.data(), j.retvals, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    HCHECK(cudaMemcpy(errmsg, j.err_msg, sizeof(errmsg), cudaMemcpyDeviceToHost));
+    errmsg[255] = 0;
+    size_t nout = offs[0] < j.out_bytes ? offs[0] : j.out_bytes;
+    size_t nerr = offs[1] < j.out_bytes ? offs[1] : j.out_bytes;
+    std::vector<char> text(nout > nerr ? nout : nerr);
+    if (nout) {
+        HCHECK(cudaMemcpy(text.data(), j.out, nout, cudaMemcpyDeviceToHost));
+        fwrite(text.data(), 1, nout, stdout);
+    }
+    fflush(stdout);
+    if (nerr) {
+        HCHECK(cudaMemcpy(text.data(), j.errout, nerr, cudaMemcpyDeviceToHost));
+        fwrite(text.data(), 1, nerr, stderr);
+    }
+    if (offs[0] > j.out_bytes || offs[1] > j.out_bytes)
+        fprintf(stderr, "GPUMPI: output truncated (raise --out-bytes)\n");
+    int exit_code = 0;
+    if (status[1] != 0) {
+        char m[400];
+        snprintf(m, sizeof(m), "job failed: error %d on rank %d: %s", status[1], status[2], errmsg);
+        set_last_error(m);
+        fprintf(stderr, "GPUMPI: %s\n", m);
+        exit_code = 1;
+    }
+    if (status[3] != n) {
+        fprintf(stderr, "GPUMPI: only %d of %d ranks finished\n", status[3], n);
+        exit_code = 1;
+    }
+    for (int r = 0; r < n; r++)
+        if (rets[r] != 0) exit_code = 1;
+    if (o.verbose) fprintf(stderr, "GPUMPI: kernel finished in %.3f s\n", now_s() - t0);
+    fflush(stderr);
+    cudaEventDestroy(done);
+    cudaStreamDestroy(st);
+    cudaFree(dslots);
+    cudaFree(dargs);
+    cudaFree(base);
+    return exit_code;
+}

@@ -1,0 +1,382 @@
+// Datatypes and reduction operators.
+//
+// Operator semantics and the (operator, type-class) legality table follow
+// gpu_libs/gpu_mpi/operators.cu:73-200: MAX/MIN on integer and floating types,
+// SUM/PROD also on complex types, LAND/LOR/LXOR on integer and logical types,
+// BAND/BOR/BXOR on integer and byte types.  MAXLOC/MINLOC, which the reference
+// declares but cannot instantiate, work here on the pair types.  Every
+// operator is applied as inout = op(in, inout) (operators.cu:216-218) and the
+// MAX/MIN tie rules are the reference's (`a > b ? a : b`, `a > b ? b : a`).
+// Logical XOR uses MPI's definition (!a != !b); it equals the reference's
+// `a != b` on 0/1 inputs.  Complex products use round-to-nearest intrinsics
+// so that no multiply-add is contracted and results match a host fold bit
+// for bit.
+#include "rt.cuh"
+
+#define GPUMPI_OP_OBJ_F(name, idx) {idx, 1, nullptr}
+#define GPUMPI_OP_OBJ_SEP ,
+__device__ MPI_Op_impl gm_builtin_ops[GPUMPI_NUM_BUILTIN_OPS] = {
+    GPUMPI_OPS_LIST(GPUMPI_OP_OBJ_F, GPUMPI_OP_OBJ_SEP)};
+#undef GPUMPI_OP_OBJ_F
+#undef GPUMPI_OP_OBJ_SEP
+
+#define GPUMPI_OP_DEF_F(name, idx) __device__ MPI_Op name = &gm_builtin_ops[idx];
+#define GPUMPI_OP_DEF_SEP
+GPUMPI_OPS_LIST(GPUMPI_OP_DEF_F, GPUMPI_OP_DEF_SEP)
+#undef GPUMPI_OP_DEF_F
+#undef GPUMPI_OP_DEF_SEP
+
+namespace gm {
+
+enum TypeClass { TC_INT, TC_FLOAT, TC_LOGICAL, TC_COMPLEX, TC_BYTE, TC_TEXT, TC_PAIR, TC_BAD };
+
+// Canonical element kinds (one template instantiation per kind).
+enum Canon {
+    K_I8, K_U8, K_I16, K_U16, K_I32, K_U32, K_I64, K_U64, K_F32, K_F64, K_BOOL, K_CF32, K_CF64,
+    K_2INT, K_FLOATINT, K_DOUBLEINT, K_LONGINT, K_OPAQUE1, K_OPAQUE4, K_BAD
+};
+
+struct TypeInfo {
+    int size;
+    int canon;
+    int cls;
+};
+
+static __device__ TypeInfo basic_info(int t) {
+    switch (t) {
+        case MPI_CHAR: return {1, K_OPAQUE1, TC_TEXT};
+        case MPI_SHORT: return {2, K_I16, TC_INT};
+        case MPI_INT: return {4, K_I32, TC_INT};
+        case MPI_LONG: return {8, K_I64, TC_INT};
+        case MPI_LONG_LONG_INT: return {8, K_I64, TC_INT};
+        case MPI_LONG_LONG: return {8, K_I64, TC_INT};
+        case MPI_SIGNED_CHAR: return {1, K_I8, TC_INT};
+        case MPI_UNSIGNED_CHAR: return {1, K_U8, TC_INT};
+        case MPI_UNSIGNED_SHORT: return {2, K_U16, TC_INT};
+        case MPI_UNSIGNED: return {4, K_U32, TC_INT};
+        case MPI_UNSIGNED_LONG: return {8, K_U64, TC_INT};
+        case MPI_UNSIGNED_LONG_LONG: return {8, K_U64, TC_INT};
+        case MPI_FLOAT: return {4, K_F32, TC_FLOAT};
+        case MPI_DOUBLE: return {8, K_F64, TC_FLOAT};
+        case MPI_LONG_DOUBLE: return {8, K_F64, TC_FLOAT};
+        case MPI_WCHAR: return {4, K_OPAQUE4, TC_TEXT};
+        case MPI_C_BOOL: return {1, K_BOOL, TC_LOGICAL};
+        case MPI_INT8_T: return {1, K_I8, TC_INT};
+        case MPI_INT16_T: return {2, K_I16, TC_INT};
+        case MPI_INT32_T: return {4, K_I32, TC_INT};
+        case MPI_INT64_T: return {8, K_I64, TC_INT};
+        case MPI_UINT8_T: return {1, K_U8, TC_INT};
+        case MPI_UINT16_T: return {2, K_U16, TC_INT};
+        case MPI_UINT32_T: return {4, K_U32, TC_INT};
+        case MPI_UINT64_T: return {8, K_U64, TC_INT};
+        case MPI_C_COMPLEX: return {8, K_CF32, TC_COMPLEX};
+        case MPI_C_FLOAT_COMPLEX: return {8, K_CF32, TC_COMPLEX};
+        case MPI_C_DOUBLE_COMPLEX: return {16, K_CF64, TC_COMPLEX};
+        case MPI_C_LONG_DOUBLE_COMPLEX: return {16, K_CF64, TC_COMPLEX};
+        case MPI_BYTE: return {1, K_U8, TC_BYTE};
+        case MPI_2INT: return {8, K_2INT, TC_PAIR};
+        case MPI_FLOAT_INT: return {8, K_FLOATINT, TC_PAIR};
+        case MPI_DOUBLE_INT: return {16, K_DOUBLEINT, TC_PAIR};
+        case MPI_LONG_INT: return {16, K_LONGINT, TC_PAIR};
+        case MPI_PACKED: return {1, K_OPAQUE1, TC_BYTE};
+        default: return {-1, K_BAD, TC_BAD};
+    }
+}
+
+__device__ int dtype_base(MPI_Datatype t, int* mult) {
+    int ti = (int)t;
+    if (ti >= 0 && ti < GPUMPI_NUM_BASIC_TYPES) {
+        *mult = 1;
+        return ti;
+    }
+    if (ti >= GPUMPI_FIRST_DERIVED_TYPE) {
+        RankPriv* p = bctx().priv;
+        int k = ti - GPUMPI_FIRST_DERIVED_TYPE;
+        if (k < p->dt_used && p->dt_count[k] >= 0) {
+            *mult = p->dt_count[k];
+            return p->dt_base[k];
+        }
+    }
+    *mult = 0;
+    return -1;
+}
+
+__device__ int dtype_size(MPI_Datatype t) {
+    int mult;
+    int b = dtype_base(t, &mult);
+    if (b < 0) return -1;
+    return basic_info(b).size * mult;
+}
+
+static __device__ bool legal(int opi, int cls) {
+    switch (opi) {
+        case 0: case 1: return cls == TC_INT || cls == TC_FLOAT;
+        case 2: case 3: return cls == TC_INT || cls == TC_FLOAT || cls == TC_COMPLEX;
+        case 4: case 6: case 8: return cls == TC_INT || cls == TC_LOGICAL;
+        case 5: case 7: case 9: return cls == TC_INT || cls == TC_BYTE;
+        case 10: case 11: return cls == TC_PAIR;
+        default: return false;
+    }
+}
+
+// MPI_SUCCESS when `op` may reduce `t`, else MPI_ERR_OP.
+__device__ int op_check(MPI_Op op, MPI_Datatype t) {
+    if (op == nullptr) return MPI_ERR_OP;
+    if (op->builtin < 0) return op->fn ? MPI_SUCCESS : MPI_ERR_OP;
+    int mult;
+    int b = dtype_base(t, &mult);
+    if (b < 0) return MPI_ERR_TYPE;
+    return legal(op->builtin, basic_info(b).cls) ? MPI_SUCCESS : MPI_ERR_OP;
+}
+
+// ---------------------------------------------------------------- operators
+template <class T> struct OMax { __device__ static T f(T a, T b) { return a > b ? a : b; } };
+template <class T> struct OMin { __device__ static T f(T a, T b) { return a > b ? b : a; } };
+template <class T> struct OSum { __device__ static T f(T a, T b) { return (T)(a + b); } };
+template <class T> struct OProd { __device__ static T f(T a, T b) { return (T)(a * b); } };
+template <class T> struct OLAnd { __device__ static T f(T a, T b) { return (T)(a && b); } };
+template <class T> struct OLOr { __device__ static T f(T a, T b) { return (T)(a || b); } };
+template <class T> struct OLXor { __device__ static T f(T a, T b) { return (T)((!a) != (!b)); } };
+template <class T> struct OBAnd { __device__ static T f(T a, T b) { return (T)(a & b); } };
+template <class T> struct OBOr { __device__ static T f(T a, T b) { return (T)(a | b); } };
+template <class T> struct OBXor { __device__ static T f(T a, T b) { return (T)(a ^ b); } };
+
+template <> struct OSum<float> { __device__ static float f(float a, float b) { return __fadd_rn(a, b); } };
+template <> struct OSum<double> { __device__ static double f(double a, double b) { return __dadd_rn(a, b); } };
+template <> struct OProd<float> { __device__ static float f(float a, float b) { return __fmul_rn(a, b); } };
+template <> struct OProd<double> { __device__ static double f(double a, double b) { return __dmul_rn(a, b); } };
+
+template <> struct OSum<gpumpi_cfloat> {
+    __device__ static gpumpi_cfloat f(gpumpi_cfloat a, gpumpi_cfloat b) {
+        return {__fadd_rn(a.re, b.re), __fadd_rn(a.im, b.im)};
+    }
+};
+template <> struct OSum<gpumpi_cdouble> {
+    __device__ static gpumpi_cdouble f(gpumpi_cdouble a, gpumpi_cdouble b) {
+        return {__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im)};
+    }
+};
+template <> struct OProd<gpumpi_cfloat> {
+    __device__ static gpumpi_cfloat f(gpumpi_cfloat a, gpumpi_cfloat b) {
+        return {__fsub_rn(__fmul_rn(a.re, b.re), __fmul_rn(a.im, b.im)),
+                __fadd_rn(__fmul_rn(a.re, b.im), __fmul_rn(a.im, b.re))};
+    }
+};
+template <> struct OProd<gpumpi_cdouble> {
+    __device__ static gpumpi_cdouble f(gpumpi_cdouble a, gpumpi_cdouble b) {
+        return {__dsub_rn(__dmul_rn(a.re, b.re), __dmul_rn(a.im, b.im)),
+                __dadd_rn(__dmul_rn(a.re, b.im), __dmul_rn(a.im, b.re))};
+    }
+};
+template <class T> struct OMaxLoc {
+    __device__ static T f(T a, T b) {
+        if (a.val > b.val) return a;
+        if (a.val < b.val) return b;
+        return a.idx < b.idx ? a : b;
+    }
+};
+template <class T> struct OMinLoc {
+    __device__ static T f(T a, T b) {
+        if (a.val > b.val) return b;
+        if (a.val < b.val) return a;
+        return a.idx < b.idx ? a : b;
+    }
+};
+
+// ---------------------------------------------------------------- fold kernels
+template <class T>
+static __device__ __forceinline__ const T* in_ptr(const Pub* pub, int q, u64 in_off) {
+    return reinterpret_cast<const T*>((const char*)ldcg(&pub[q].sbuf) + in_off);
+}
+
+// Scalar path: any element type, any alignment.
+template <class T, class O>
+static __device__ void fold_scalar(T* out, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
+                                   int tid, int T_) {
+    for (u64 i = lo + tid; i < hi; i += T_) {
+        T acc = ldcg(in_ptr<T>(pub, 0, in_off) + i);
+        for (int q = 1; q < nin; q++) acc = O::f(ldcg(in_ptr<T>(pub, q, in_off) + i), acc);
+        out[i - lo] = acc;
+    }
+}
+
+// 16-byte vector path for 4- and 8-byte element types when every input and
+// the output are 16-byte aligned at element lo.  Four independent vectors per
+// thread keep 64 bytes per thread in flight for every input rank.
+template <class T, class O>
+static __device__ void fold_vec(T* out, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
+                                int tid, int T_) {
+    constexpr int V = 16 / sizeof(T);
+    constexpr int U = 4;
+    const u64 n = hi - lo;
+    const u64 nvec = n / V;
+    uint4* ov = reinterpret_cast<uint4*>(out);
+    u64 v = tid;
+    for (; v + (U - 1) * (u64)T_ < nvec; v += (u64)U * T_) {
+        uint4 acc[U];
+        const uint4* b0 = reinterpret_cast<const uint4*>(in_ptr<T>(pub, 0, in_off) + lo);
+#pragma unroll
+        for (int k = 0; k < U; k++) acc[k] = __ldcg(b0 + v + (u64)k * T_);
+        for (int q = 1; q < nin; q++) {
+            const uint4* bq = reinterpret_cast<const uint4*>(in_ptr<T>(pub, q, in_off) + lo);
+            uint4 x[U];
+#pragma unroll
+            for (int k = 0; k < U; k++) x[k] = __ldcg(bq + v + (u64)k * T_);
+#pragma unroll
+            for (int k = 0; k < U; k++) {
+                T* a = reinterpret_cast<T*>(&acc[k]);
+                const T* xe = reinterpret_cast<const T*>(&x[k]);
+#pragma unroll
+                for (int e = 0; e < V; e++) a[e] = O::f(xe[e], a[e]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) ov[v + (u64)k * T_] = acc[k];
+    }
+    for (; v < nvec; v += T_) {
+        uint4 acc = __ldcg(reinterpret_cast<const uint4*>(in_ptr<T>(pub, 0, in_off) + lo) + v);
+        for (int q = 1; q < nin; q++) {
+            uint4 x = __ldcg(reinterpret_cast<const uint4*>(in_ptr<T>(pub, q, in_off) + lo) + v);
+            T* a = reinterpret_cast<T*>(&acc);
+            const T* xe = reinterpret_cast<const T*>(&x);
+#pragma unroll
+            for (int e = 0; e < V; e++) a[e] = O::f(xe[e], a[e]);
+        }
+        ov[v] = acc;
+    }
+    const u64 done = nvec * V;
+    if (done < n) fold_scalar<T, O>(out + done, pub, nin, in_off, lo + done, hi, tid, T_);
+}
+
+template <class T, class O>
+static __device__ void fold_t(void* outv, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
+                              int tid, int T_) {
+    T* out = reinterpret_cast<T*>(outv);
+    if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
+        bool aligned = ((uintptr_t)out & 15) == 0;
+        for (int q = 0; q < nin && aligned; q++)
+            aligned = (((uintptr_t)(in_ptr<T>(pub, q, in_off) + lo)) & 15) == 0;
+        if (aligned) {
+            fold_vec<T, O>(out, pub, nin, in_off, lo, hi, tid, T_);
+            return;
+        }
+    }
+    fold_scalar<T, O>(out, pub, nin, in_off, lo, hi, tid, T_);
+}
+
+template <template <class> class O>
+static __device__ void fold_numeric(int canon, void* out, const Pub* pub, int nin, u64 in_off,
+                                    u64 lo, u64 hi, int tid, int T_) {
+    switch (canon) {
+        case K_I8: fold_t<signed char, O<signed char>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_U8: fold_t<unsigned char, O<unsigned char>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_I16: fold_t<short, O<short>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_U16: fold_t<unsigned short, O<unsigned short>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_I32: fold_t<int, O<int>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_U32: fold_t<unsigned, O<unsigned>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_I64: fold_t<long long, O<long long>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_U64: fold_t<unsigned long long, O<unsigned long long>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        default: break;
+    }
+}
+
+template <template <class> class O>
+static __device__ void fold_float(int canon, void* out, const Pub* pub, int nin, u64 in_off,
+                                  u64 lo, u64 hi, int tid, int T_) {
+    if (canon == K_F32) fold_t<float, O<float>>(out, pub, nin, in_off, lo, hi, tid, T_);
+    else if (canon == K_F64) fold_t<double, O<double>>(out, pub, nin, in_off, lo, hi, tid, T_);
+}
+
+static __device__ void fold_user(MPI_User_function* fn, MPI_Datatype dt, int es, void* out,
+                                 const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi, int tid,
+                                 int T_) {
+    // Contiguous chunks per thread; each chunk folds in rank order.
+    const u64 n = hi - lo;
+    const u64 per = (n + T_ - 1) / T_;
+    const u64 c0 = (u64)tid * per;
+    if (c0 >= n) return;
+    u64 c1 = c0 + per;
+    if (c1 > n) c1 = n;
+    char* o = (char*)out + c0 * es;
+    const char* i0 = (const char*)ldcg(&pub[0].sbuf) + in_off + (lo + c0) * es;
+    for (u64 k = 0; k < (c1 - c0) * es; k++) o[k] = __ldcg(i0 + k);
+    int len = (int)(c1 - c0);
+    MPI_Datatype d = dt;
+    for (int q = 1; q < nin; q++) {
+        const char* iq = (const char*)ldcg(&pub[q].sbuf) + in_off + (lo + c0) * es;
+        fn((void*)iq, o, &len, &d);
+    }
+}
+
+__device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, int esize, void* out, const Pub* pub, int nin,
+                           u64 in_off, u64 lo, u64 hi, int tid, int T_) {
+    if (hi <= lo || nin <= 0) {
+        bsync();
+        return;
+    }
+    if (opi < 0) {
+        fold_user(ufn, base, esize, out, pub, nin, in_off, lo, hi, tid, T_);
+        bsync();
+        return;
+    }
+    const int canon = basic_info((int)base).canon;
+    switch (opi) {
+        case 0:
+            fold_numeric<OMax>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_float<OMax>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 1:
+            fold_numeric<OMin>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_float<OMin>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 2:
+            fold_numeric<OSum>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_float<OSum>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_CF32) fold_t<gpumpi_cfloat, OSum<gpumpi_cfloat>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_CF64) fold_t<gpumpi_cdouble, OSum<gpumpi_cdouble>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 3:
+            fold_numeric<OProd>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_float<OProd>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_CF32) fold_t<gpumpi_cfloat, OProd<gpumpi_cfloat>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_CF64) fold_t<gpumpi_cdouble, OProd<gpumpi_cdouble>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 4:
+            fold_numeric<OLAnd>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_BOOL) fold_t<bool, OLAnd<bool>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 5: fold_numeric<OBAnd>(canon, out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case 6:
+            fold_numeric<OLOr>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_BOOL) fold_t<bool, OLOr<bool>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 7: fold_numeric<OBOr>(canon, out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case 8:
+            fold_numeric<OLXor>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            if (canon == K_BOOL) fold_t<bool, OLXor<bool>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            break;
+        case 9: fold_numeric<OBXor>(canon, out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case 10:
+        case 11: {
+            const bool mx = opi == 10;
+            if (canon == K_2INT) {
+                if (mx) fold_t<gpumpi_2int, OMaxLoc<gpumpi_2int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                else fold_t<gpumpi_2int, OMinLoc<gpumpi_2int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            } else if (canon == K_FLOATINT) {
+                if (mx) fold_t<gpumpi_float_int, OMaxLoc<gpumpi_float_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                else fold_t<gpumpi_float_int, OMinLoc<gpumpi_float_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            } else if (canon == K_DOUBLEINT) {
+                if (mx) fold_t<gpumpi_double_int, OMaxLoc<gpumpi_double_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                else fold_t<gpumpi_double_int, OMinLoc<gpumpi_double_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            } else if (canon == K_LONGINT) {
+                if (mx) fold_t<gpumpi_long_int, OMaxLoc<gpumpi_long_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                else fold_t<gpumpi_long_int, OMinLoc<gpumpi_long_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            }
+            break;
+        }
+        default: break;
+    }
+    bsync();
+}
+
+}  // namespace gm

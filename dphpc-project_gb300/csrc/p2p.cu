@@ -1,0 +1,391 @@
+// Point-to-point engine: per-receiver HBM mailboxes with warp-ballot matching,
+// eager delivery into mailbox slots for small messages and receiver-pull
+// rendezvous for large ones.  All functions here are block-cooperative: every
+// thread of the rank block calls them with its thread index.
+//
+// Ownership rule: thread 0 (the rank's leader) is the only thread that reads
+// or writes rank-private state (request objects, the posted-receive and
+// deferred-send lists).  It hands the block what it needs -- match keys,
+// copy source/destination/length -- through shared memory (bctx().x), so the
+// other threads never load memory the leader wrote.  Data written by other
+// ranks (mailbox headers, payloads) is read through L2 (ld.global.cg) after
+// an acquire load of the mailbox's ready mask.
+//
+// Semantics follow the reference transport (gpu_libs/gpu_libc/cuda_mpi.cu:
+// 120-471: match-or-enqueue, progress of all pending operations in order)
+// with its defects corrected:
+//  * a send completes only once its bytes are in the mailbox (eager) or in
+//    the receiver's buffer (rendezvous), never by lending the sender's buffer
+//    (cuda_mpi.cu:176-212);
+//  * wildcard source/tag match arrived messages as well as posted ones
+//    (cuda_mpi.cu:300-304);
+//  * messages between one sender and one receiver on one communicator match
+//    in send order: the arrival stamp is taken after the slot is claimed, and a
+//    sender publishes its messages one after the other, so the lowest matching
+//    stamp is always the oldest message of that sender;
+//  * every wait is bounded and returns an error code instead of spinning forever.
+#include "rt.cuh"
+
+namespace gm {
+
+static __device__ __forceinline__ char* eager_slot(Job* j, int world_rank, int slot) {
+    return j->eager + ((u64)world_rank * MB_SLOTS + slot) * j->eager_bytes;
+}
+
+// Thread 0: claim a free slot in the destination's mailbox and fill its header.
+// Returns the slot, or -1 when the mailbox is full.
+static __device__ int claim_and_fill(Job* j, MPI_Request_impl* r) {
+    Mailbox* mb = &j->mbox[r->peer_world];
+    u64 used = ld_relaxed(&mb->used);
+    int s;
+    for (;;) {
+        u64 freeb = ~used;
+        if (freeb == 0) return -1;
+        s = __ffsll((long long)freeb) - 1;
+        u64 bit = 1ull << s;
+        u64 old = atomicOr(&mb->used, bit);
+        if (!(old & bit)) break;
+        used = old | bit;
+    }
+    u64 stamp = atomicAdd(&mb->stamp, 1ull);
+    MsgHdr& h = mb->hdr[s];
+    const bool eager = r->bytes <= j->eager_bytes;
+    h.ctx = r->ctx;
+    h.src = r->src_rank;
+    h.tag = r->tag;
+    h.kind = eager ? 0 : 1;
+    h.bytes = r->bytes;
+    h.stamp = stamp;
+    h.rdv_src = eager ? nullptr : r->buf;
+    h.rdv_done = eager ? nullptr : (u32*)&r->done;
+    return s;
+}
+
+// Thread 0: describe the eager copy of request r into `slot` in bctx().x.
+static __device__ void stage_delivery(MPI_Request_impl* r, int slot) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    const bool eager = r->bytes <= j->eager_bytes;
+    b.x.slot = slot;
+    b.x.src = r->buf;
+    b.x.dst = slot >= 0 ? eager_slot(j, r->peer_world, slot) : nullptr;
+    b.x.bytes = (slot >= 0 && eager) ? r->bytes : 0;
+    b.x.peer = r->peer_world;
+    b.x.a = eager;
+}
+
+// All threads: copy the staged eager payload, then thread 0 publishes the slot.
+static __device__ void deliver_staged(MPI_Request_impl* r, int tid, int T) {
+    BlockCtx& b = bctx();
+    const void* src = b.x.src;
+    void* dst = b.x.dst;
+    const u64 n = b.x.bytes;
+    const int slot = b.x.slot, peer = b.x.peer, eager = b.x.a;
+    if (n) blk_copy(dst, src, n, tid, T);
+    bsync();
+    if (tid == 0) {
+        r->state = eager ? RS_DONE : RS_WAIT_RDV;
+        __threadfence();
+        atom_or_release(&b.job->mbox[peer].ready, 1ull << slot);
+    }
+}
+
+static __device__ void list_append(RankPriv* p, int* head, int* tail, int idx) {
+    p->reqs[idx].next = -1;
+    if (*tail >= 0) p->reqs[*tail].next = idx;
+    else *head = idx;
+    *tail = idx;
+}
+
+__device__ int p2p_send_start(MPI_Request_impl* r, int tid, int T) {
+    BlockCtx& b = bctx();
+    bsync();
+    if (tid == 0) {
+        RankPriv* p = b.priv;
+        int slot = -1;
+        r->done = 0;
+        if (p->defer_head < 0) slot = claim_and_fill(b.job, r);
+        if (slot < 0) {
+            r->state = RS_DEFERRED;
+            list_append(p, &p->defer_head, &p->defer_tail, r->index);
+        }
+        stage_delivery(r, slot);
+    }
+    bsync();
+    if (b.x.slot >= 0) deliver_staged(r, tid, T);
+    return MPI_SUCCESS;
+}
+
+// Warp 0 finds the earliest ready message matching the keys in bctx().x
+// (ctx/peer/tag) among the slots of `ready`; the result is valid in lane 0.
+static __device__ int warp_match(u64 ready, int tid) {
+    BlockCtx& b = bctx();
+    int best = -1;
+    if (tid < 32) {
+        const int ctx = b.x.ctx, src = b.x.peer, tag = b.x.tag;
+        Mailbox* mb = &b.job->mbox[b.rank];
+        u64 best_stamp = ~0ull;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const int s = tid + 32 * k;
+            if ((ready >> s) & 1ull) {
+                const MsgHdr* h = &mb->hdr[s];
+                const int hctx = __ldcg(&h->ctx), hsrc = __ldcg(&h->src), htag = __ldcg(&h->tag);
+                if (hctx == ctx && (src == MPI_ANY_SOURCE || hsrc == src) &&
+                    (tag == MPI_ANY_TAG || htag == tag)) {
+                    const u64 st = __ldcg(&h->stamp);
+                    if (st < best_stamp) {
+                        best_stamp = st;
+                        best = s;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const u64 os = __shfl_xor_sync(0xffffffffu, best_stamp, off);
+            const int ob = __shfl_xor_sync(0xffffffffu, best, off);
+            if (os < best_stamp) {
+                best_stamp = os;
+                best = ob;
+            }
+        }
+    }
+    return best;
+}
+
+// One pass over posted receives, in posting order, against one snapshot of the
+// ready mask.  Thread 0 walks the list; for each receive the block matches
+// and, on a hit, copies.  Every message of the snapshot goes to the earliest
+// posted receive it matches, which is MPI's matching rule.
+static __device__ int progress_recvs(int tid, int T) {
+    BlockCtx& b = bctx();
+    RankPriv* p = b.priv;
+    Mailbox* mb = &b.job->mbox[b.rank];
+    int did = 0;
+    // thread-0 walk state
+    int cur = -1, prev = -1;
+    u64 ready = 0;
+    if (tid == 0) {
+        ready = ld_acquire(&mb->ready);
+        cur = ready ? p->recv_head : -1;
+    }
+    for (;;) {
+        bsync();
+        if (tid == 0) {
+            b.x.a = cur >= 0;
+            if (cur >= 0) {
+                const MPI_Request_impl* r = &p->reqs[cur];
+                b.x.ctx = r->ctx;
+                b.x.peer = r->peer;
+                b.x.tag = r->tag;
+                b.bval = ready;
+            }
+        }
+        bsync();
+        if (!b.x.a) break;
+        const int best = warp_match(b.bval, tid);
+        bsync();
+        if (tid == 0) {
+            b.x.slot = best;
+            if (best >= 0) {
+                const MPI_Request_impl* r = &p->reqs[cur];
+                const MsgHdr* h = &mb->hdr[best];
+                const u64 bytes = __ldcg(&h->bytes);
+                const int kind = __ldcg(&h->kind);
+                b.x.src = kind == 0 ? (const void*)eager_slot(b.job, b.rank, best) : ldcg(&h->rdv_src);
+                b.x.dst = r->buf;
+                b.x.bytes = bytes < r->bytes ? bytes : r->bytes;
+            }
+        }
+        bsync();
+        const int slot = b.x.slot;
+        if (slot >= 0) {
+            blk_copy(b.x.dst, b.x.src, b.x.bytes, tid, T);
+            bsync();
+            if (tid == 0) {
+                MPI_Request_impl* r = &p->reqs[cur];
+                const MsgHdr* h = &mb->hdr[slot];
+                const u64 bytes = __ldcg(&h->bytes);
+                const int kind = __ldcg(&h->kind);
+                r->st_source = __ldcg(&h->src);
+                r->st_tag = __ldcg(&h->tag);
+                r->st_bytes = bytes < r->bytes ? bytes : r->bytes;
+                r->st_err = bytes > r->bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
+                u32* done = kind == 1 ? ldcg(&h->rdv_done) : nullptr;
+                atomicAnd(&mb->ready, ~(1ull << slot));
+                if (done) {
+                    __threadfence();
+                    st_release32(done, 1u);
+                }
+                __threadfence();
+                atomicAnd(&mb->used, ~(1ull << slot));
+                r->state = RS_DONE;
+                const int nxt = r->next;
+                if (prev >= 0) p->reqs[prev].next = nxt;
+                else p->recv_head = nxt;
+                if (p->recv_tail == cur) p->recv_tail = prev;
+                cur = nxt;
+                // The pass keeps its snapshot: a message that arrived after it
+                // was taken must go to the earliest matching receive, which
+                // this pass may already have walked past; the next pass starts
+                // again at the head of the list.
+                ready &= ~(1ull << slot);
+                if (!ready) cur = -1;
+            }
+            did = 1;
+        } else if (tid == 0) {
+            prev = cur;
+            cur = p->reqs[cur].next;
+        }
+    }
+    return did;
+}
+
+// Retry sends that found the destination mailbox full, oldest first.
+static __device__ int progress_deferred(int tid, int T) {
+    BlockCtx& b = bctx();
+    RankPriv* p = b.priv;
+    int did = 0;
+    for (;;) {
+        bsync();
+        if (tid == 0) {
+            int slot = -1;
+            const int h = p->defer_head;
+            b.x.c = h;
+            if (h >= 0) {
+                MPI_Request_impl* r = &p->reqs[h];
+                slot = claim_and_fill(b.job, r);
+                if (slot >= 0) {
+                    p->defer_head = r->next;
+                    if (p->defer_head < 0) p->defer_tail = -1;
+                }
+                stage_delivery(r, slot);
+            } else {
+                b.x.slot = -1;
+            }
+        }
+        bsync();
+        if (b.x.slot < 0) break;
+        deliver_staged(&p->reqs[b.x.c], tid, T);
+        did = 1;
+    }
+    return did;
+}
+
+__device__ int p2p_progress(int tid, int T, int* did_work) {
+    int d1 = progress_deferred(tid, T);
+    int d2 = progress_recvs(tid, T);
+    if (did_work) *did_work = d1 | d2;
+    return MPI_SUCCESS;
+}
+
+__device__ int p2p_recv_post(MPI_Request_impl* r, int tid, int T) {
+    BlockCtx& b = bctx();
+    if (tid == 0) {
+        RankPriv* p = b.priv;
+        r->state = RS_POSTED;
+        list_append(p, &p->recv_head, &p->recv_tail, r->index);
+    }
+    progress_recvs(tid, T);
+    return MPI_SUCCESS;
+}
+
+static __device__ __forceinline__ int req_is_done(MPI_Request_impl* r) {
+    if (r->state == RS_DONE) return 1;
+    if (r->state == RS_WAIT_RDV && ld_acquire32((const u32*)&r->done)) {
+        r->state = RS_DONE;
+        return 1;
+    }
+    return 0;
+}
+
+// Thread 0: abort / timeout check of a wait loop.  Returns an error code or 0.
+static __device__ int wait_check(u64 t0, int did, unsigned* ns, const char* what) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    if (job_aborted(j)) {
+        int code = ld_acquire_int(&j->status[1]);
+        return code ? code : GPUMPI_ERR_ABORTED;
+    }
+    if (gtime() - t0 > j->timeout_ns) {
+        job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, what);
+        return GPUMPI_ERR_TIMEOUT;
+    }
+    if (!did) {
+        __nanosleep(*ns);
+        if (*ns < 256) *ns <<= 1;
+    } else {
+        *ns = 32;
+    }
+    return 0;
+}
+
+// Progress until r completes (blocking) or for one pass (non-blocking).
+// Non-blocking calls report completion in call.a[1].
+__device__ int p2p_wait(MPI_Request_impl* r, int tid, int T, int blocking) {
+    BlockCtx& b = bctx();
+    u64 t0 = 0;
+    unsigned ns = 32;
+    if (tid == 0) t0 = gtime();
+    for (int iter = 0;; iter++) {
+        int done = (int)bcast(tid == 0 ? req_is_done(r) : 0, tid);
+        if (done || (!blocking && iter > 0)) {
+            if (!blocking && tid == 0) b.call.a[1] = (u64)done;
+            return MPI_SUCCESS;
+        }
+        int did = 0;
+        p2p_progress(tid, T, &did);
+        int code = 0;
+        if (tid == 0 && blocking) code = wait_check(t0, did, &ns, "point-to-point wait timed out");
+        code = (int)bcast(code, tid);
+        if (code) return code;
+    }
+}
+
+// Look for a matching arrived message without receiving it.  Thread 0 (the
+// leader) writes the status, so it may live in the leader's local memory.
+__device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status* st, int tid,
+                         int T) {
+    BlockCtx& b = bctx();
+    Mailbox* mb = &b.job->mbox[b.rank];
+    u64 t0 = 0;
+    unsigned ns = 32;
+    if (tid == 0) t0 = gtime();
+    for (;;) {
+        int did = progress_deferred(tid, T);
+        bsync();
+        if (tid == 0) {
+            b.bval = ld_acquire(&mb->ready);
+            b.x.ctx = ctx;
+            b.x.peer = source;
+            b.x.tag = tag;
+        }
+        bsync();
+        const int best = b.bval ? warp_match(b.bval, tid) : -1;
+        int found = 0;
+        if (tid == 0 && best >= 0) {
+            const MsgHdr* h = &mb->hdr[best];
+            if (st) {
+                const u64 hb = __ldcg(&h->bytes);
+                st->MPI_SOURCE = __ldcg(&h->src);
+                st->MPI_TAG = __ldcg(&h->tag);
+                st->MPI_ERROR = MPI_SUCCESS;
+                st->gpumpi_count_lo = (int)(hb & 0xffffffffu);
+                st->gpumpi_count_hi = (int)(hb >> 32);
+            }
+            found = 1;
+        }
+        found = (int)bcast(found, tid);
+        if (found || !blocking) {
+            if (tid == 0) b.call.a[1] = (u64)found;
+            return MPI_SUCCESS;
+        }
+        int code = 0;
+        if (tid == 0) code = wait_check(t0, did, &ns, "probe timed out");
+        code = (int)bcast(code, tid);
+        if (code) return code;
+    }
+}
+
+}  // namespace gm

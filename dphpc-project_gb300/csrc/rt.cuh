@@ -1,0 +1,543 @@
+// Internal data layout and primitives of the GB300 device MPI runtime.
+//
+// Execution model.  One MPI rank is one thread block of T threads (T a
+// multiple of 32, >= 64).  The converted program's scalar code runs on thread
+// 0 of the block (the leader).  The other T-1 threads wait on named barrier 1;
+// every MPI call the leader makes is written to shared memory and executed by
+// all T threads together (`block_call` / `dispatch`).  This replaces the
+// one-thread-per-rank model of gpu_libs/gpu_main/main.cu:103-131, where every
+// copy was a single-thread memcpy (gpu_libs/gpu_libc/cuda_mpi.cu:168).
+//
+// Memory.  All runtime state lives in plain device memory (HBM), never in
+// managed memory, and synchronises with GPU-scope release/acquire operations.
+// The reference kept it in managed memory with system-scope atomics
+// (cuda_mpi.cuh:78-113, :459-533).
+//
+// Waiting.  Every spin-wait is bounded by the job's timeout (%globaltimer)
+// and by the job's abort flag; on expiry the call returns an error code and
+// the job is marked failed.  Nothing traps.
+#pragma once
+
+#include <stdint.h>
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#include "mpi.cuh"
+
+namespace gm {
+
+typedef unsigned long long u64;
+typedef unsigned int u32;
+
+// ----------------------------------------------------------------- limits
+constexpr int MB_SLOTS = 64;             // mailbox slots per receiving rank (one u64 mask)
+constexpr int MAX_COMMS = 64;            // live communicator handles per rank
+constexpr int MAX_GROUPS = 64;           // live group handles per rank
+constexpr int MAX_DTYPES = 64;           // derived datatypes per rank
+constexpr int STAGE_BYTES = 64 * 1024;   // per-rank scratch for staging local-memory buffers
+constexpr int OUT_LINE_MAX = 1024;       // longest formatted line kept whole
+constexpr int COLL_SCRATCH_BYTES = 64 * 1024;
+
+// ----------------------------------------------------------------- calls
+enum CallOp : int {
+    OP_EXIT = 0,
+    OP_SEND_START,
+    OP_RECV_POST,
+    OP_WAIT,
+    OP_TEST,
+    OP_PROBE,
+    OP_BARRIER,
+    OP_BCAST,
+    OP_REDUCE,
+    OP_ALLREDUCE,
+    OP_GATHERV,
+    OP_SCATTERV,
+    OP_ALLGATHERV,
+    OP_ALLTOALLV,
+    OP_REDUCE_SCATTER_BLOCK,
+    OP_SCAN,
+    OP_COMM_SPLIT,
+    OP_COMM_DUP,
+    OP_MEMCPY,
+    OP_MEMSET,
+    OP_FINALIZE,
+    OP_NUM
+};
+
+
+// ----------------------------------------------------------------- p2p
+// Header of a message waiting in a receiver's mailbox slot.
+struct MsgHdr {
+    int ctx;
+    int src;            // sender's rank in the communicator
+    int tag;
+    int kind;           // 0 = eager (payload in the slot), 1 = rendezvous (payload at rdv_src)
+    u64 bytes;
+    u64 stamp;          // arrival order at this receiver
+    const void* rdv_src;
+    u32* rdv_done;      // sender's completion word for rendezvous
+    u64 pad[2];
+};
+static_assert(sizeof(MsgHdr) == 64, "MsgHdr layout");
+
+// Per-receiver mailbox.  Senders claim a slot by setting its bit in `used`,
+// fill the header (and the eager payload), then set the bit in `ready` with
+// release semantics.  Only the receiver clears bits.
+struct alignas(128) Mailbox {
+    u64 used;
+    u64 pad0[15];
+    u64 ready;
+    u64 pad1[15];
+    u64 stamp;
+    u64 pad2[15];
+    MsgHdr hdr[MB_SLOTS];
+};
+
+enum ReqKind : int { RK_FREE = 0, RK_SEND = 1, RK_RECV = 2 };
+enum ReqState : int { RS_NEW = 0, RS_DEFERRED, RS_POSTED, RS_WAIT_RDV, RS_DONE };
+
+}  // namespace gm
+
+// Request object (MPI_Request is a pointer to it).  Pooled per rank.
+struct MPI_Request_impl {
+    int kind;
+    int state;
+    int peer;           // comm rank of destination / source (or MPI_ANY_SOURCE)
+    int tag;
+    int ctx;
+    int peer_world;     // job rank of the destination (sends)
+    int src_rank;       // own rank in the communicator (sends)
+    int index;          // position in the rank's pool
+    void* buf;          // engine-side buffer, always global memory
+    void* user_buf;     // caller's buffer when it was staged (local memory), else == buf
+    gm::u64 bytes;      // send size or receive capacity
+    gm::u64 stage_alloc;// nonzero when buf came from the heap for staging
+    volatile gm::u32 done;  // rendezvous completion, written by the receiver
+    int next;           // link in the posted-receive / deferred-send list
+    int st_source;
+    int st_tag;
+    int st_err;
+    gm::u64 st_bytes;
+    int persistent;
+    int pad;
+};
+
+namespace gm {
+
+// ----------------------------------------------------------------- collectives
+// Buffers a rank exposes to its peers for one collective call.
+struct Pub {
+    const void* sbuf;
+    void* rbuf;
+    const int* scounts;
+    const int* sdispls;
+    const int* rcounts;
+    const int* rdispls;
+    long long a0;
+    long long a1;
+};
+
+__device__ __forceinline__ Pub load_pub(const Pub* p) {
+    Pub v;
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(&v);
+#pragma unroll
+    for (int i = 0; i < 8; i++) d[i] = __ldcg(s + i);
+    return v;
+}
+
+// Communicator state shared by all members.  `arrive`, `mid` and `depart`
+// hold, per member, the sequence number of the latest collective the member
+// reached the corresponding point of.  Each member writes only its own entry,
+// so no collective needs an atomic read-modify-write.
+struct alignas(128) CommShared {
+    int size;
+    int ctx;
+    int* members;       // job rank of each member; nullptr means identity (WORLD)
+    Pub* pub;           // [size]
+    u64* arrive;        // [size]
+    u64* mid;           // [size]
+    u64* depart;        // [size]
+    u64 split_ptr;      // scratch used while creating a child communicator
+    int topo_ndims;     // Cartesian topology (0 = none)
+    int topo_dims[8];
+    int topo_periods[8];
+};
+
+}  // namespace gm
+
+struct MPI_Comm_impl {
+    int kind;           // 0 free, 1 live handle, 2 WORLD sentinel, 3 SELF sentinel
+    int ctx;
+    int size;
+    int rank;
+    int refcnt;
+    int pad;
+    gm::CommShared* cs;
+    gm::u64 seq;        // collectives entered on this communicator
+};
+
+struct MPI_Group_impl {
+    int kind;           // 0 free, 1 live, 2 WORLD sentinel, 3 EMPTY sentinel
+    int n;
+    int* ranks;         // job ranks, heap allocated (nullptr for identity)
+    int refcnt;
+    int pad;
+};
+
+struct MPI_Op_impl {
+    int builtin;        // 0..11 for predefined operators, -1 for user functions
+    int commute;
+    MPI_User_function* fn;
+};
+
+namespace gm {
+
+struct Heap;
+
+// Per-rank state touched only by the rank's own block.
+struct RankPriv {
+    MPI_Request_impl* reqs;
+    int nreqs;
+    int free_head;
+    int recv_head, recv_tail;      // posted, unmatched receives, in posting order
+    int defer_head, defer_tail;    // sends waiting for a mailbox slot, in order
+    int initialized, finalized;
+    int errno_v;
+    int opt_ind, opt_err, opt_opt, opt_pos;
+    char* opt_arg;
+    char* strtok_save;
+    u64 rng;
+    unsigned int rnd[34];          // rand() state: additive-feedback generator
+    int rnd_i;
+    int rnd_seeded;
+    char* stage;                   // STAGE_BYTES of global scratch
+    int stage_off;
+    int exited;
+    MPI_Comm_impl comms[MAX_COMMS];    // [0] = WORLD, [1] = SELF
+    MPI_Group_impl groups[MAX_GROUPS];
+    int dt_count[MAX_DTYPES];          // derived contiguous types: count of base
+    int dt_base[MAX_DTYPES];
+    int dt_used;
+};
+
+// Slab allocator instance (see gmalloc.cu).
+struct Heap {
+    char* base;
+    u64 bytes;
+    u32 npages;
+    u32 pad;
+    struct PageMeta* meta;        // [npages]
+    u32* cls_pages;               // [NCLS * npages], 0xffffffff = empty entry
+    u32* cls_count;               // [NCLS]
+    u32* cls_hint;                // [NCLS * 32]
+    u32* next_page;               // bump pointer (1 word)
+    u64* large_free;              // [LARGE_BUCKETS] tagged stack heads
+    u32* stats;                   // [8] counters
+};
+
+// One MPI job (a converted program instance with its own MPI_COMM_WORLD).
+struct Job {
+    int id;
+    int nranks;
+    int first_slot;
+    int threads;                  // threads per rank block
+    int argc;
+    int max_requests;
+    char** argv;
+    u64 timeout_ns;
+    u64 eager_bytes;
+    Mailbox* mbox;                // [nranks]
+    char* eager;                  // [nranks * MB_SLOTS * eager_bytes]
+    RankPriv* priv;               // [nranks]
+    MPI_Request_impl* reqpool;    // [nranks * max_requests]
+    char* stage;                  // [nranks * STAGE_BYTES]
+    CommShared* world_cs;
+    CommShared* self_cs;          // [nranks]
+    char* arena;                  // bump arena for communicator state
+    u64 arena_bytes;
+    u64* arena_off;
+    Heap heap;
+    char* out;                    // formatted stdout text, appended in arrival order
+    u64 out_bytes;
+    u64* out_off;
+    char* errout;                 // formatted stderr text
+    u64* errout_off;
+    char* coll_scratch;           // [nranks * COLL_SCRATCH_BYTES]
+    int* status;                  // [0] abort flag, [1] first error code, [2] error rank, [3] ranks done,
+                                  // [4] ranks finalized, [5] ctx counter, [6] exit code of any exit()
+    int* retvals;                 // [nranks]
+    char* err_msg;                // 256 bytes
+    u64 t0_ns;                    // %globaltimer at launch
+};
+
+// Where a thread block finds its job: slot -> (job, rank).
+struct Launch {
+    Job* jobs;
+    int njobs;
+    int nslots;
+    int* slot_job;                // [nslots], -1 = idle
+    int* slot_rank;               // [nslots]
+};
+
+
+// ----------------------------------------------------------------- primitives
+__device__ __forceinline__ u64 gtime() {
+    u64 t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Block barriers use the non-aligned `barrier.sync` form: the leader thread
+// (lane 0 of warp 0) arrives from user code while lanes 1-31 of its warp
+// arrive from the helper loop, which the aligned `bar.sync` does not allow.
+__device__ __forceinline__ void bar_named(int id, int nthreads) {
+    asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+// Block-wide OR of a predicate (non-aligned barrier 3).
+__device__ __forceinline__ int bar_or(int pred, int nthreads) {
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\t"
+        "barrier.red.or.pred q, 3, %2, p;\n\tselp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(pred), "r"(nthreads)
+        : "memory");
+    return r;
+}
+
+__device__ __forceinline__ u64 ld_acquire(const u64* p) {
+    u64 v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ u32 ld_acquire32(const u32* p) {
+    u32 v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_acquire_int(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(u64* p, u64 v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_release32(u32* p, u32 v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ u64 atom_or_release(u64* p, u64 v) {
+    u64 old;
+    asm volatile("atom.release.gpu.global.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ u64 ld_relaxed(const u64* p) {
+    u64 v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ bool is_global(const void* p) { return __isGlobal(p) != 0; }
+
+// Loads of data written by other rank blocks go through L2 (ld.global.cg), so
+// a line this SM cached for an earlier message in the same slot or table entry
+// can never be returned.
+template <class T>
+__device__ __forceinline__ T ldcg(const T* p) {
+    if constexpr (sizeof(T) == 1) {
+        unsigned char v = __ldcg(reinterpret_cast<const unsigned char*>(p));
+        return *reinterpret_cast<T*>(&v);
+    } else if constexpr (sizeof(T) == 2) {
+        unsigned short v = __ldcg(reinterpret_cast<const unsigned short*>(p));
+        return *reinterpret_cast<T*>(&v);
+    } else if constexpr (sizeof(T) == 4) {
+        unsigned int v = __ldcg(reinterpret_cast<const unsigned int*>(p));
+        return *reinterpret_cast<T*>(&v);
+    } else if constexpr (sizeof(T) == 8) {
+        unsigned long long v = __ldcg(reinterpret_cast<const unsigned long long*>(p));
+        return *reinterpret_cast<T*>(&v);
+    } else if constexpr (sizeof(T) == 16 && alignof(T) >= 8) {
+        ulonglong2 v;
+        v.x = __ldcg(reinterpret_cast<const unsigned long long*>(p));
+        v.y = __ldcg(reinterpret_cast<const unsigned long long*>(p) + 1);
+        return *reinterpret_cast<T*>(&v);
+    } else {
+        T v;
+        unsigned char* d = reinterpret_cast<unsigned char*>(&v);
+        const unsigned char* s = reinterpret_cast<const unsigned char*>(p);
+        for (unsigned i = 0; i < sizeof(T); i++) d[i] = __ldcg(s + i);
+        return v;
+    }
+}
+
+// Arguments of a collective call (all buffers global memory).
+struct CollArgs {
+    MPI_Comm_impl* comm;
+    const void* sbuf;
+    void* rbuf;
+    const int* scounts;
+    const int* sdispls;
+    const int* rcounts;
+    const int* rdispls;
+    u64 count;          // elements (Bcast/Reduce/Allreduce/Scan) or per-block counts
+    int ssize;          // element size of the send type
+    int rsize;          // element size of the receive type
+    MPI_Datatype dtype; // base type for reductions
+    MPI_Op op;
+    int opi;            // builtin operator index, -1 for a user function
+    MPI_User_function* ufn;
+    int root;
+    int algo;           // 0 = choose automatically
+    long long a0, a1;
+};
+// Arguments of one block-wide call, in shared memory.
+struct Call {
+    int op;
+    int ret;
+    union {
+        u64 a[16];
+        CollArgs ca;
+    };
+};
+
+// Block-wide context, at offset 0 of dynamic shared memory.
+struct BlockCtx {
+    Job* job;
+    RankPriv* priv;
+    int rank;                     // rank in the job (MPI_COMM_WORLD rank)
+    int slot;
+    int T;                        // threads in the block
+    int leader_mode;              // 1: thread 0 runs user code, others are helpers
+    Call call;
+    int bflag;                    // scratch broadcast words
+    int bflag2;
+    u64 bval;
+    u64 bval2;
+    int match_slot;
+    int err;
+    long long bcv;                // value broadcast by bcast()
+    // Values thread 0 hands to the whole block (thread 0 alone reads and
+    // writes rank-private state: requests, lists, communicator handles).
+    struct Xfer {
+        const void* src;
+        void* dst;
+        u64 bytes;
+        int ctx, peer, tag, next;
+        int slot, a, b, c;
+    } x;
+    // The communicator of the running collective, as read by thread 0.
+    struct CommView {
+        CommShared* shared;
+        Pub* pub;
+        u64* arrive;
+        u64* mid;
+        u64* depart;
+        int P;
+        int me;
+        u64 seq;
+    } cv;
+    int in_call;                  // leader is inside block_call (helpers busy)
+};
+
+__device__ __forceinline__ BlockCtx& bctx() {
+    extern __shared__ __align__(16) char gm_dsmem[];
+    return *reinterpret_cast<BlockCtx*>(gm_dsmem);
+}
+
+// Intra-call barrier of all threads of the rank block.
+__device__ __forceinline__ void bsync() { bar_named(2, bctx().T); }
+
+// Broadcast a value computed on thread 0 to every thread of the block.  The
+// leading barrier guarantees all threads have consumed the previous value.
+__device__ __forceinline__ long long bcast(long long x, int tid) {
+    BlockCtx& b = bctx();
+    bsync();
+    if (tid == 0) b.bcv = x;
+    bsync();
+    return b.bcv;
+}
+__device__ __forceinline__ long long pack2(int hi, int lo) {
+    return (long long)(((unsigned long long)(unsigned)hi << 32) | (unsigned)lo);
+}
+__device__ __forceinline__ int unpack_hi(long long v) { return (int)((unsigned long long)v >> 32); }
+__device__ __forceinline__ int unpack_lo(long long v) { return (int)(unsigned)(unsigned long long)v; }
+
+// ----------------------------------------------------------------- job status
+__device__ __forceinline__ bool job_aborted(const Job* j) {
+    return ld_acquire_int(&j->status[0]) != 0;
+}
+// Record the first error of the job (code, rank, message) and raise the abort flag.
+__device__ void job_fail(Job* j, int rank, int code, const char* msg);
+
+// Bounded wait helpers.  Return MPI_SUCCESS, GPUMPI_ERR_TIMEOUT or GPUMPI_ERR_ABORTED.
+__device__ int wait_ge(const u64* addr, u64 target);
+__device__ int wait_flags_ge(const u64* flags, int n, u64 target, int skip, int tid, int T);
+__device__ int wait_u32_nonzero(const volatile u32* addr);
+
+// ----------------------------------------------------------------- copies
+// Block-cooperative copy of n bytes between global buffers.
+__device__ void blk_copy(void* dst, const void* src, u64 n, int tid, int T);
+__device__ void blk_memset(void* dst, int c, u64 n, int tid, int T);
+// Same, using only the 32 lanes of one warp.
+__device__ void warp_copy(void* dst, const void* src, u64 n, int lane);
+
+// ----------------------------------------------------------------- leader side
+__device__ int block_call(Call& c);
+__device__ void helper_loop();
+__device__ int dispatch_all(int tid);   // executed by every thread of the block
+
+// Staging of local-memory buffers (leader thread only).
+__device__ void* stage_temp(int bytes);
+__device__ void stage_reset();
+
+// Resolve a handle to the calling rank's communicator object.
+__device__ MPI_Comm_impl* comm_resolve(MPI_Comm c);
+__device__ __forceinline__ int comm_world_rank(const MPI_Comm_impl* c, int r) {
+    return c->cs->members ? __ldcg(&c->cs->members[r]) : r;
+}
+
+// datatypes / operators
+__device__ int dtype_size(MPI_Datatype t);
+__device__ int dtype_base(MPI_Datatype t, int* mult);
+__device__ int op_check(MPI_Op op, MPI_Datatype t);
+struct Pub;
+// Rank-order fold of elements [lo, hi): out[i - lo] = acc with acc = in_0[i];
+// acc = op(in_q[i], acc) for q = 1..nin-1, where in_q = pub[q].sbuf + in_off bytes.
+__device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, int esize, void* out, const Pub* pub, int nin,
+                           u64 in_off, u64 lo, u64 hi, int tid, int T);
+
+// p2p engine (block-cooperative)
+__device__ int p2p_send_start(MPI_Request_impl* r, int tid, int T);
+__device__ int p2p_recv_post(MPI_Request_impl* r, int tid, int T);
+__device__ int p2p_progress(int tid, int T, int* did_work);
+__device__ int p2p_wait(MPI_Request_impl* r, int tid, int T, int blocking);
+__device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status* st, int tid, int T);
+
+// collective engine (block-cooperative); all buffers are global memory
+
+
+__device__ int coll_barrier(MPI_Comm_impl* c, int tid, int T);
+__device__ int coll_bcast(const CollArgs& a, int tid, int T);
+__device__ int coll_reduce(const CollArgs& a, int tid, int T);
+__device__ int coll_allreduce(const CollArgs& a, int tid, int T);
+__device__ int coll_gatherv(const CollArgs& a, int tid, int T);
+__device__ int coll_scatterv(const CollArgs& a, int tid, int T);
+__device__ int coll_allgatherv(const CollArgs& a, int tid, int T);
+__device__ int coll_alltoallv(const CollArgs& a, int tid, int T);
+__device__ int coll_alltoall(const CollArgs& a, int tid, int T);
+__device__ int coll_reduce_scatter_block(const CollArgs& a, int tid, int T);
+__device__ int coll_scan(const CollArgs& a, int exclusive, int tid, int T);
+__device__ int comm_split_block(MPI_Comm_impl* parent, int color, int key, MPI_Comm_impl** out,
+                                int tid, int T);
+
+// heap
+__device__ void* heap_alloc(Heap* h, u64 bytes);
+__device__ void heap_free(Heap* h, void* p);
+__device__ u64 heap_usable_size(Heap* h, void* p);
+
+// rank lifecycle
+__device__ void rank_init(int tid, int T);
+__device__ void rank_finish(int rc);
+__device__ int out_write(Job* j, int stream, const char* s, int n);   // stream 1 stdout, 2 stderr
+__device__ void rank_exit_now(int status);   // end the calling rank (leader thread) immediately
+
+}  // namespace gm

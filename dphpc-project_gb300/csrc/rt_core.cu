@@ -1,0 +1,342 @@
+// Core of the device runtime: handle sentinels, job status and bounded waits,
+// the block-cooperative copy engine, the leader/helper call protocol and the
+// per-rank lifecycle.
+#include "rt.cuh"
+
+// ---------------------------------------------------------------- sentinels
+// MPI_COMM_WORLD / MPI_COMM_SELF / MPI_GROUP_WORLD / MPI_GROUP_EMPTY are the
+// addresses of these objects; every rank resolves them to its own job.
+__device__ MPI_Comm_impl gm_world_sentinel = {2, 0, 0, 0, 0, 0, nullptr, 0};
+__device__ MPI_Comm_impl gm_self_sentinel = {3, 0, 0, 0, 0, 0, nullptr, 0};
+__device__ MPI_Group_impl gm_group_world_sentinel = {2, 0, nullptr, 0, 0};
+__device__ MPI_Group_impl gm_group_empty_sentinel = {3, 0, nullptr, 0, 0};
+
+__device__ MPI_Comm MPI_COMM_WORLD = &gm_world_sentinel;
+__device__ MPI_Comm MPI_COMM_SELF = &gm_self_sentinel;
+__device__ MPI_Comm MPI_COMM_NULL = nullptr;
+__device__ MPI_Group MPI_GROUP_WORLD = &gm_group_world_sentinel;
+__device__ MPI_Group MPI_GROUP_EMPTY = &gm_group_empty_sentinel;
+__device__ MPI_Group MPI_GROUP_NULL = nullptr;
+
+namespace gm {
+
+// ---------------------------------------------------------------- job status
+__device__ void job_fail(Job* j, int rank, int code, const char* msg) {
+    if (atomicCAS(&j->status[1], 0, code) == 0) {
+        j->status[2] = rank;
+        int i = 0;
+        if (msg) {
+            for (; i < 255 && msg[i]; i++) j->err_msg[i] = msg[i];
+        }
+        j->err_msg[i] = 0;
+    }
+    __threadfence();
+    atomicExch(&j->status[0], 1);
+}
+
+static __device__ __forceinline__ int wait_fail(Job* j) {
+    int code = ld_acquire_int(&j->status[1]);
+    return code ? code : GPUMPI_ERR_ABORTED;
+}
+
+__device__ int wait_ge(const u64* addr, u64 target) {
+    if (ld_acquire(addr) >= target) return MPI_SUCCESS;
+    Job* j = bctx().job;
+    u64 t0 = gtime();
+    unsigned ns = 32;
+    for (;;) {
+        if (ld_acquire(addr) >= target) return MPI_SUCCESS;
+        if (job_aborted(j)) return wait_fail(j);
+        if (gtime() - t0 > j->timeout_ns) {
+            job_fail(j, bctx().rank, GPUMPI_ERR_TIMEOUT, "collective wait timed out");
+            return GPUMPI_ERR_TIMEOUT;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+    }
+}
+
+__device__ int wait_u32_nonzero(const volatile u32* addr) {
+    if (*addr) return MPI_SUCCESS;
+    Job* j = bctx().job;
+    u64 t0 = gtime();
+    unsigned ns = 32;
+    for (;;) {
+        if (ld_acquire32((const u32*)addr)) return MPI_SUCCESS;
+        if (job_aborted(j)) return wait_fail(j);
+        if (gtime() - t0 > j->timeout_ns) {
+            job_fail(j, bctx().rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
+            return GPUMPI_ERR_TIMEOUT;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+    }
+}
+
+// All threads of the block poll a slice of `flags` (every entry except `skip`)
+// until each is >= target.  Returns the same code on every thread.
+__device__ int wait_flags_ge(const u64* flags, int n, u64 target, int skip, int tid, int T) {
+    int rc = MPI_SUCCESS;
+    for (int q = tid; q < n; q += T) {
+        if (q == skip) continue;
+        rc = wait_ge(&flags[q], target);
+        if (rc) break;
+    }
+    int failed = bar_or(rc != MPI_SUCCESS, T);
+    if (!failed) return MPI_SUCCESS;
+    return wait_fail(bctx().job);
+}
+
+// ---------------------------------------------------------------- copies
+template <class V, int U>
+static __device__ __forceinline__ void copy_vec(V* __restrict__ d, const V* __restrict__ s, u64 nv,
+                                                u64 tid, u64 T) {
+    u64 i = tid;
+    for (; i + (U - 1) * T < nv; i += U * T) {
+        V r[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) r[k] = __ldcg(s + i + k * T);
+#pragma unroll
+        for (int k = 0; k < U; k++) d[i + k * T] = r[k];
+    }
+    for (; i < nv; i += T) d[i] = __ldcg(s + i);
+}
+
+static __device__ __forceinline__ void copy_range(char* d, const char* s, u64 n, u64 tid, u64 T) {
+    uintptr_t da = (uintptr_t)d, sa = (uintptr_t)s;
+    if (((da ^ sa) & 15) == 0) {
+        u64 head = (16 - (da & 15)) & 15;
+        if (head > n) head = n;
+        for (u64 i = tid; i < head; i += T) d[i] = __ldcg(s + i);
+        d += head;
+        s += head;
+        n -= head;
+        u64 nv = n >> 4;
+        copy_vec<uint4, 8>((uint4*)d, (const uint4*)s, nv, tid, T);
+        u64 done = nv << 4;
+        for (u64 i = done + tid; i < n; i += T) d[i] = __ldcg(s + i);
+    } else if (((da ^ sa) & 7) == 0) {
+        u64 head = (8 - (da & 7)) & 7;
+        if (head > n) head = n;
+        for (u64 i = tid; i < head; i += T) d[i] = __ldcg(s + i);
+        d += head;
+        s += head;
+        n -= head;
+        u64 nv = n >> 3;
+        copy_vec<uint2, 8>((uint2*)d, (const uint2*)s, nv, tid, T);
+        u64 done = nv << 3;
+        for (u64 i = done + tid; i < n; i += T) d[i] = __ldcg(s + i);
+    } else if (((da ^ sa) & 3) == 0) {
+        u64 head = (4 - (da & 3)) & 3;
+        if (head > n) head = n;
+        for (u64 i = tid; i < head; i += T) d[i] = __ldcg(s + i);
+        d += head;
+        s += head;
+        n -= head;
+        u64 nv = n >> 2;
+        copy_vec<unsigned int, 8>((unsigned int*)d, (const unsigned int*)s, nv, tid, T);
+        u64 done = nv << 2;
+        for (u64 i = done + tid; i < n; i += T) d[i] = __ldcg(s + i);
+    } else {
+        for (u64 i = tid; i < n; i += T) d[i] = __ldcg(s + i);
+    }
+}
+
+__device__ void blk_copy(void* dst, const void* src, u64 n, int tid, int T) {
+    if (n == 0 || dst == src) return;
+    copy_range((char*)dst, (const char*)src, n, (u64)tid, (u64)T);
+}
+
+__device__ void warp_copy(void* dst, const void* src, u64 n, int lane) {
+    if (n == 0 || dst == src) return;
+    copy_range((char*)dst, (const char*)src, n, (u64)lane, 32);
+}
+
+__device__ void blk_memset(void* dst, int c, u64 n, int tid, int T) {
+    char* d = (char*)dst;
+    unsigned char b = (unsigned char)c;
+    uintptr_t da = (uintptr_t)d;
+    u64 head = (16 - (da & 15)) & 15;
+    if (head > n) head = n;
+    for (u64 i = tid; i < head; i += T) d[i] = b;
+    d += head;
+    n -= head;
+    u64 nv = n >> 4;
+    unsigned w = b * 0x01010101u;
+    uint4 v = make_uint4(w, w, w, w);
+    uint4* dv = (uint4*)d;
+    for (u64 i = tid; i < nv; i += T) dv[i] = v;
+    for (u64 i = (nv << 4) + tid; i < n; i += T) d[i] = b;
+}
+
+// ---------------------------------------------------------------- call protocol
+__device__ int block_call(Call& c) {
+    BlockCtx& b = bctx();
+    b.call = c;
+    b.in_call = 1;
+    bar_named(1, b.T);
+    int rc = dispatch_all(0);
+    bar_named(1, b.T);
+    b.in_call = 0;
+    c = b.call;
+    return rc;
+}
+
+__device__ void helper_loop() {
+    BlockCtx& b = bctx();
+    const int tid = threadIdx.x;
+    for (;;) {
+        bar_named(1, b.T);
+        if (b.call.op == OP_EXIT) break;
+        dispatch_all(tid);
+        bar_named(1, b.T);
+    }
+}
+
+// ---------------------------------------------------------------- staging
+__device__ void* stage_temp(int bytes) {
+    RankPriv* p = bctx().priv;
+    int off = (p->stage_off + 15) & ~15;
+    if (off + bytes > STAGE_BYTES) return nullptr;
+    p->stage_off = off + bytes;
+    return p->stage + off;
+}
+__device__ void stage_reset() { bctx().priv->stage_off = 0; }
+
+// ---------------------------------------------------------------- handles
+__device__ MPI_Comm_impl* comm_resolve(MPI_Comm c) {
+    RankPriv* p = bctx().priv;
+    if (c == &gm_world_sentinel) return &p->comms[0];
+    if (c == &gm_self_sentinel) return &p->comms[1];
+    if (c == nullptr) return nullptr;
+    if (c < &p->comms[0] || c >= &p->comms[MAX_COMMS]) return nullptr;
+    if (c->kind != 1) return nullptr;
+    return c;
+}
+
+// ---------------------------------------------------------------- output
+__device__ int out_write(Job* j, int stream, const char* s, int n) {
+    if (n <= 0) return 0;
+    char* buf = stream == 2 ? j->errout : j->out;
+    u64* offp = stream == 2 ? j->errout_off : j->out_off;
+    u64 off = atomicAdd(offp, (u64)n);
+    if (off >= j->out_bytes) return 0;
+    u64 m = n;
+    if (off + m > j->out_bytes) m = j->out_bytes - off;
+    for (u64 i = 0; i < m; i++) buf[off + i] = s[i];
+    return (int)m;
+}
+
+// ---------------------------------------------------------------- lifecycle
+__device__ void rank_init(int tid, int T) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    RankPriv* p = b.priv;
+    const int r = b.rank;
+    MPI_Request_impl* reqs = j->reqpool + (u64)r * j->max_requests;
+    // Rank-private state is written and read by thread 0 only.
+    if (tid == 0) {
+        for (int i = 0; i < j->max_requests; i++) {
+            reqs[i].kind = RK_FREE;
+            reqs[i].state = RS_NEW;
+            reqs[i].index = i;
+            reqs[i].next = (i + 1 < j->max_requests) ? i + 1 : -1;
+        }
+        for (int i = 0; i < MAX_COMMS; i++) p->comms[i].kind = 0;
+        for (int i = 0; i < MAX_GROUPS; i++) p->groups[i].kind = 0;
+        p->reqs = reqs;
+        p->nreqs = j->max_requests;
+        p->free_head = j->max_requests > 0 ? 0 : -1;
+        p->recv_head = p->recv_tail = -1;
+        p->defer_head = p->defer_tail = -1;
+        p->initialized = 0;
+        p->finalized = 0;
+        p->errno_v = 0;
+        p->opt_ind = 1;
+        p->opt_err = 1;
+        p->opt_opt = 0;
+        p->opt_pos = 0;
+        p->opt_arg = nullptr;
+        p->strtok_save = nullptr;
+        p->rng = 0x9E3779B97F4A7C15ull ^ ((u64)r * 0xD1B54A32D192ED03ull);
+        p->stage = j->stage + (u64)r * STAGE_BYTES;
+        p->stage_off = 0;
+        p->exited = 0;
+        p->dt_used = 0;
+        MPI_Comm_impl& w = p->comms[0];
+        w.kind = 1;
+        w.ctx = 1;
+        w.size = j->nranks;
+        w.rank = r;
+        w.refcnt = 1;
+        w.cs = j->world_cs;
+        w.seq = 0;
+        MPI_Comm_impl& s = p->comms[1];
+        s.kind = 1;
+        s.ctx = 2;
+        s.size = 1;
+        s.rank = 0;
+        s.refcnt = 1;
+        s.cs = &j->self_cs[r];
+        s.seq = 0;
+    }
+    __syncthreads();
+}
+
+// End the calling rank from the leader thread: record the status, release the
+// helper threads (they leave the kernel) and retire the leader with PTX `exit`.
+__device__ void rank_exit_now(int status) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    b.priv->exited = 1;
+    if (status != 0) {
+        atomicCAS(&j->status[6], 0, status);
+        job_fail(j, b.rank, GPUMPI_ERR_ABORTED, "a rank called exit() or abort() with nonzero status");
+    }
+    rank_finish(status);
+    if (b.leader_mode && !b.in_call) {
+        b.call.op = OP_EXIT;
+        bar_named(1, b.T);
+    }
+    asm volatile("exit;");
+}
+
+__device__ void rank_finish(int rc) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    j->retvals[b.rank] = rc;
+    __threadfence();
+    atomicAdd(&j->status[3], 1);
+}
+
+}  // namespace gm
+
+namespace gm {
+
+// Block set-up for program kernels: find this slot's job and rank, then
+// initialise the rank.  Returns false for idle slots.
+__device__ bool program_block_begin(const Launch& L) {
+    BlockCtx& b = bctx();
+    const int slot = blockIdx.x;
+    if (threadIdx.x == 0) {
+        const int jid = slot < L.nslots ? L.slot_job[slot] : -1;
+        if (jid < 0) {
+            b.job = nullptr;
+        } else {
+            b.job = &L.jobs[jid];
+            b.rank = L.slot_rank[slot];
+            b.priv = &b.job->priv[b.rank];
+            b.slot = slot;
+            b.T = (int)blockDim.x;
+            b.leader_mode = 1;
+            b.in_call = 0;
+            b.call.op = -1;
+        }
+    }
+    __syncthreads();
+    if (!b.job) return false;
+    rank_init((int)threadIdx.x, (int)blockDim.x);
+    return true;
+}
+
+}  // namespace gm

@@ -1,0 +1,75 @@
+"""Host-side helpers for the GB300 device MPI runtime.
+
+Builds the CUDA runtime, the program binaries and the CPU oracle, runs
+programs through the C-ABI launcher (each program executable is a thin
+`main` around `gpumpi_main`), and binds the host collective C ABI of
+libgpumpi.so with ctypes.  The product path is the CUDA runtime: nothing here
+falls back to the CPU; loading libgpumpi.so fails loudly if it is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from dataclasses import dataclass
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+BUILD = os.path.join(PKG, "build")
+BIN = os.path.join(BUILD, "bin")
+ORACLE = os.path.join(ROOT, "oracle")
+ORACLE_BIN = os.path.join(ORACLE, "build", "bin")
+LIB = os.path.join(BUILD, "libgpumpi.so")
+
+
+def _jobs() -> int:
+    return max(1, min(32, os.cpu_count() or 1))
+
+
+def build(verbose: bool = False) -> None:
+    """Compile the CUDA runtime and programs (sm_103a) and the CPU oracle."""
+    out = None if verbose else subprocess.PIPE
+    for d in (PKG, ORACLE):
+        r = subprocess.run(["make", "-C", d, f"-j{_jobs()}"], stdout=out, stderr=subprocess.STDOUT,
+                           text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout or "")
+            raise RuntimeError(f"build failed in {d}")
+
+
+@dataclass
+class RunResult:
+    returncode: int
+    stdout: str
+    stderr: str
+
+    def lines(self, prefix: str = "") -> list[str]:
+        return [ln for ln in self.stdout.splitlines() if ln.startswith(prefix)]
+
+
+def _run(exe: str, args: list[str], nranks: int, extra: list[str], timeout: float) -> RunResult:
+    if not os.path.exists(exe):
+        raise FileNotFoundError(f"{exe} is not built; run build() first")
+    cmd = [exe, *args, "---gpumpi", "-n", str(nranks), *extra]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+    return RunResult(r.returncode, r.stdout, r.stderr)
+
+
+def run_program(name: str, args: list[str] | None = None, nranks: int = 2,
+                extra: list[str] | None = None, timeout: float = 300.0) -> RunResult:
+    """Run a converted program on the GPU (one rank per thread block)."""
+    return _run(os.path.join(BIN, name), args or [], nranks, extra or [], timeout)
+
+
+def run_oracle(name: str, args: list[str] | None = None, nranks: int = 2,
+               extra: list[str] | None = None, timeout: float = 300.0) -> RunResult:
+    """Run the same program on host cores through the hostmpi oracle."""
+    return _run(os.path.join(ORACLE_BIN, name), args or [], nranks, extra or [], timeout)
+
+
+def load_library() -> ctypes.CDLL:
+    """Load libgpumpi.so (the host collective C ABI)."""
+    if not os.path.exists(LIB):
+        raise FileNotFoundError(f"{LIB} missing: the CUDA runtime is not built")
+    return ctypes.CDLL(LIB, mode=ctypes.RTLD_GLOBAL)

@@ -1,0 +1,368 @@
+// Known-answer point-to-point scenarios, restating the patterns of the
+// reference's tests/cuda_mpi_test.cu (single int :5-36, 16-int array :38-73,
+// bidirectional exchange :75-127, repeated sizes with distinct tags :129-174,
+// 3-rank ring flood :177-233, 10-rank all-to-all x20 :235-317) through the
+// MPI API, plus wildcard, probe, status and rendezvous-size cases.
+// Every rank prints "<scenario> rank <r> ok <0|1>".
+// Usage: kat_p2p <scenario> ---gpumpi -n <ranks>
+#include "global_vars.cuh"
+#include "mpi.h.cuh"
+#include "stdio.h.cuh"
+#include "stdlib.h.cuh"
+#include "string.h.cuh"
+
+__device__ int single_int(int rank) {
+    int ok = 1;
+    if (rank == 0) {
+        int x = 3456;
+        MPI_Send(&x, 1, MPI_INT, 1, 15, MPI_COMM_WORLD);
+    } else if (rank == 1) {
+        int x = 0;
+        MPI_Recv(&x, 1, MPI_INT, 0, 15, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+        ok = x == 3456;
+    }
+    return ok;
+}
+
+__device__ int array16(int rank) {
+    int ok = 1;
+    int x[16];
+    if (rank == 0) {
+        for (int i = 0; i < 16; i++) x[i] = i;
+        MPI_Send(x, 16, MPI_INT, 1, 15, MPI_COMM_WORLD);
+    } else if (rank == 1) {
+        for (int i = 0; i < 16; i++) x[i] = 0;
+        MPI_Recv(x, 16, MPI_INT, 0, 15, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+        for (int i = 0; i < 16; i++)
+            if (x[i] != i) ok = 0;
+    }
+    return ok;
+}
+
+__device__ int sendrecv(int rank) {
+    int ok = 1;
+    int x[16], y[16];
+    MPI_Request req[2];
+    int other = 1 - rank;
+    for (int i = 0; i < 16; i++) {
+        x[i] = rank == 0 ? i : -i;
+        y[i] = 0;
+    }
+    MPI_Irecv(y, 16, MPI_INT, other, 15, MPI_COMM_WORLD, &req[0]);
+    MPI_Isend(x, 16, MPI_INT, other, 15, MPI_COMM_WORLD, &req[1]);
+    MPI_Wait(&req[0], MPI_STATUS_IGNORE);
+    for (int i = 0; i < 16; i++)
+        if (y[i] != (rank == 0 ? -i : i)) ok = 0;
+    MPI_Wait(&req[1], MPI_STATUS_IGNORE);
+    return ok;
+}
+
+__device__ int repeat_sizes(int rank) {
+    const int reps = 5, n = 1 << (reps - 1);
+    int other = (rank + 1) % 2;
+    int local[16], remote[16];
+    MPI_Request sreq[5], rreq[5];
+    for (int i = 0; i < n; i++) {
+        local[i] = (rank + 1) * i;
+        remote[i] = 0;
+    }
+    for (int i = 0; i < reps; i++) {
+        MPI_Isend(local, 1 << i, MPI_INT, other, i + 10, MPI_COMM_WORLD, &sreq[i]);
+        MPI_Irecv(remote, 1 << i, MPI_INT, other, i + 10, MPI_COMM_WORLD, &rreq[i]);
+    }
+    for (int i = 0; i < reps; i++) {
+        MPI_Wait(&sreq[i], MPI_STATUS_IGNORE);
+        MPI_Wait(&rreq[i], MPI_STATUS_IGNORE);
+    }
+    int ok = 1;
+    for (int i = 0; i < n; i++)
+        if (remote[i] != (other + 1) * i) ok = 0;
+    return ok;
+}
+
+__device__ int flood(int rank, int size) {
+    const int reps = 5, n = 1 << (reps - 1);
+    int next = (rank + 1) % size, prev = (size + rank - 1) % size;
+    int local[16], pd[16], nd[16];
+    MPI_Request sn[5], rn[5], sp[5], rp[5];
+    for (int i = 0; i < n; i++) {
+        local[i] = (rank + 1) * i;
+        pd[i] = nd[i] = 0;
+    }
+    for (int i = 0; i < reps; i++) {
+        int tag = i + 10;
+        MPI_Isend(local, 1 << i, MPI_INT, next, tag, MPI_COMM_WORLD, &sn[i]);
+        MPI_Irecv(nd, 1 << i, MPI_INT, next, tag, MPI_COMM_WORLD, &rn[i]);
+        MPI_Isend(local, 1 << i, MPI_INT, prev, tag, MPI_COMM_WORLD, &sp[i]);
+        MPI_Irecv(pd, 1 << i, MPI_INT, prev, tag, MPI_COMM_WORLD, &rp[i]);
+    }
+    for (int i = 0; i < reps; i++) {
+        MPI_Wait(&rp[i], MPI_STATUS_IGNORE);
+        MPI_Wait(&sn[i], MPI_STATUS_IGNORE);
+        MPI_Wait(&sp[i], MPI_STATUS_IGNORE);
+        MPI_Wait(&rn[i], MPI_STATUS_IGNORE);
+    }
+    int ok = 1;
+    for (int i = 0; i < n; i++) {
+        if (pd[i] != (prev + 1) * i) ok = 0;
+        if (nd[i] != (next + 1) * i) ok = 0;
+    }
+    return ok;
+}
+
+__device__ int all_to_all(int rank, int size, int reps, int distinct) {
+    const int n = 16;
+    int* local = (int*)malloc(sizeof(int) * n * reps * size);
+    int* remote = (int*)malloc(sizeof(int) * n * reps * size);
+    MPI_Request* sreq = (MPI_Request*)malloc(sizeof(MPI_Request) * reps * size);
+    MPI_Request* rreq = (MPI_Request*)malloc(sizeof(MPI_Request) * reps * size);
+    MPI_Comm comm;
+    int drc = MPI_Comm_dup(MPI_COMM_WORLD, &comm);
+    int dsz = -1, drk = -1;
+    MPI_Comm_size(comm, &dsz);
+    MPI_Comm_rank(comm, &drk);
+    if (drc != MPI_SUCCESS || dsz != size || drk != rank)
+        printf("all_to_all rank %d: Comm_dup rc %d size %d rank %d\n", rank, drc, dsz, drk);
+    for (int r = 0; r < size; r++)
+        for (int k = 0; k < reps; k++)
+            for (int i = 0; i < n; i++) {
+                int idx = i + k * n + r * n * reps;
+                local[idx] = i * k * r;
+                remote[idx] = 0;
+            }
+    for (int k = 0; k < reps; k++)
+        for (int r = 0; r < size; r++)
+            if (r != rank) {
+                int idx = k * n + r * n * reps;
+                int tag = distinct ? 15 + k : 15;
+                MPI_Isend(local + idx, n, MPI_INT, r, tag, comm, &sreq[r + k * size]);
+                MPI_Irecv(remote + idx, n, MPI_INT, r, tag, comm, &rreq[r + k * size]);
+            }
+    for (int k = 0; k < reps; k++)
+        for (int r = 0; r < size; r++)
+            if (r != rank) {
+                MPI_Status st;
+                MPI_Wait(&sreq[r + k * size], MPI_STATUS_IGNORE);
+                MPI_Wait(&rreq[r + k * size], &st);
+                if (st.MPI_SOURCE != r) {
+                    printf("all_to_all status rank %d from %d rep %d: source %d tag %d\n", rank, r, k,
+                           st.MPI_SOURCE, st.MPI_TAG);
+                }
+            }
+    int ok = 1;
+    for (int k = 0; k < reps; k++)
+        for (int r = 0; r < size; r++)
+            if (r != rank)
+                for (int i = 0; i < n; i++)
+                    if (remote[i + k * n + r * n * reps] != i * k * rank) {
+                        if (ok)
+                            printf("all_to_all mismatch rank %d from %d rep %d elem %d: got %d want %d\n",
+                                   rank, r, k, i, remote[i + k * n + r * n * reps], i * k * rank);
+                        ok = 0;
+                    }
+    MPI_Comm_free(&comm);
+    free(local);
+    free(remote);
+    free(sreq);
+    free(rreq);
+    return ok;
+}
+
+
+// Message-identity variant of all_to_all: payload = (sender, rep, receiver, ...).
+__device__ int a2a_ids(int rank, int size, int reps) {
+    const int n = 16;
+    int* local = (int*)malloc(sizeof(int) * n * reps * size);
+    int* remote = (int*)malloc(sizeof(int) * n * reps * size);
+    MPI_Request* sreq = (MPI_Request*)malloc(sizeof(MPI_Request) * reps * size);
+    MPI_Request* rreq = (MPI_Request*)malloc(sizeof(MPI_Request) * reps * size);
+    for (int r = 0; r < size; r++)
+        for (int k = 0; k < reps; k++)
+            for (int i = 0; i < n; i++) {
+                int idx = i + k * n + r * n * reps;
+                local[idx] = i == 0 ? rank : (i == 1 ? k : (i == 2 ? r : 1000 * rank + k));
+                remote[idx] = -1;
+            }
+    for (int k = 0; k < reps; k++)
+        for (int r = 0; r < size; r++)
+            if (r != rank) {
+                int idx = k * n + r * n * reps;
+                MPI_Isend(local + idx, n, MPI_INT, r, 15, MPI_COMM_WORLD, &sreq[r + k * size]);
+                MPI_Irecv(remote + idx, n, MPI_INT, r, 15, MPI_COMM_WORLD, &rreq[r + k * size]);
+            }
+    for (int k = 0; k < reps; k++)
+        for (int r = 0; r < size; r++)
+            if (r != rank) {
+                MPI_Wait(&sreq[r + k * size], MPI_STATUS_IGNORE);
+                MPI_Wait(&rreq[r + k * size], MPI_STATUS_IGNORE);
+            }
+    int ok = 1;
+    for (int k = 0; k < reps; k++)
+        for (int r = 0; r < size; r++)
+            if (r != rank) {
+                int* m = remote + k * n + r * n * reps;
+                if (m[0] != r || m[1] != k || m[2] != rank || m[3] != 1000 * r + k) {
+                    printf("a2a_ids rank %d slot(from %d rep %d) got (sender %d rep %d dest %d tail %d)\n", rank, r,
+                           k, m[0], m[1], m[2], m[3]);
+                    ok = 0;
+                }
+            }
+    free(local);
+    free(remote);
+    free(sreq);
+    free(rreq);
+    return ok;
+}
+
+// Wildcard receives posted after the messages arrived (the reference ignored
+// wildcards on arrived messages), with filled status and MPI_Get_count.
+__device__ int wildcard(int rank, int size) {
+    int ok = 1;
+    if (rank != 0) {
+        int v[3] = {rank, rank * 10, rank * 100};
+        MPI_Send(v, rank % 3 + 1, MPI_INT, 0, 100 + rank, MPI_COMM_WORLD);
+    }
+    MPI_Barrier(MPI_COMM_WORLD);
+    if (rank == 0) {
+        int seen = 0;
+        for (int k = 1; k < size; k++) {
+            int v[3] = {0, 0, 0};
+            MPI_Status st;
+            MPI_Recv(v, 3, MPI_INT, MPI_ANY_SOURCE, MPI_ANY_TAG, MPI_COMM_WORLD, &st);
+            int cnt = -1;
+            MPI_Get_count(&st, MPI_INT, &cnt);
+            int src = st.MPI_SOURCE;
+            if (src < 1 || src >= size) ok = 0;
+            else {
+                if (st.MPI_TAG != 100 + src) ok = 0;
+                if (cnt != src % 3 + 1) ok = 0;
+                if (v[0] != src) ok = 0;
+                if (cnt > 1 && v[1] != src * 10) ok = 0;
+                seen |= 1 << src;
+            }
+        }
+        if (seen != ((1 << size) - 2)) ok = 0;
+    }
+    return ok;
+}
+
+// Probe then receive a message of unknown length; non-overtaking between
+// one sender and one receiver with equal tags.
+__device__ int probe_order(int rank, int size) {
+    int ok = 1;
+    if (rank == 1) {
+        for (int k = 0; k < 8; k++) {
+            int* v = (int*)malloc(sizeof(int) * (k + 1));
+            for (int i = 0; i <= k; i++) v[i] = k;
+            MPI_Send(v, k + 1, MPI_INT, 0, 7, MPI_COMM_WORLD);
+            free(v);
+        }
+    } else if (rank == 0) {
+        for (int k = 0; k < 8; k++) {
+            MPI_Status st;
+            MPI_Probe(1, 7, MPI_COMM_WORLD, &st);
+            int cnt = 0;
+            MPI_Get_count(&st, MPI_INT, &cnt);
+            if (cnt != k + 1) ok = 0;
+            int* v = (int*)malloc(sizeof(int) * (cnt > 0 ? cnt : 1));
+            MPI_Recv(v, cnt, MPI_INT, 1, 7, MPI_COMM_WORLD, &st);
+            for (int i = 0; i < cnt; i++)
+                if (v[i] != k) ok = 0;
+            free(v);
+        }
+        int flag = 1;
+        MPI_Iprobe(MPI_ANY_SOURCE, MPI_ANY_TAG, MPI_COMM_WORLD, &flag, MPI_STATUS_IGNORE);
+        if (flag) ok = 0;
+    }
+    (void)size;
+    return ok;
+}
+
+// Messages above the eager threshold (rendezvous), in both directions at
+// once with Sendrecv, and a ring shift with Sendrecv_replace.
+__device__ int large(int rank, int size) {
+    const int n = 1 << 18;  // 1 MiB of ints
+    int ok = 1;
+    int* a = (int*)malloc(sizeof(int) * n);
+    int* b = (int*)malloc(sizeof(int) * n);
+    for (int i = 0; i < n; i++) {
+        a[i] = rank * 1000003 + i;
+        b[i] = -1;
+    }
+    int next = (rank + 1) % size, prev = (rank + size - 1) % size;
+    MPI_Status st;
+    MPI_Sendrecv(a, n, MPI_INT, next, 3, b, n, MPI_INT, prev, 3, MPI_COMM_WORLD, &st);
+    for (int i = 0; i < n; i++)
+        if (b[i] != prev * 1000003 + i) {
+            ok = 0;
+            break;
+        }
+    if (st.MPI_SOURCE != prev || st.MPI_TAG != 3) ok = 0;
+    MPI_Sendrecv_replace(a, n, MPI_INT, next, 4, prev, 4, MPI_COMM_WORLD, &st);
+    for (int i = 0; i < n; i++)
+        if (a[i] != prev * 1000003 + i) {
+            ok = 0;
+            break;
+        }
+    free(a);
+    free(b);
+    return ok;
+}
+
+// Waitany / Waitsome / Testall over a batch of receives.
+__device__ int completion(int rank, int size) {
+    int ok = 1;
+    const int k = 6;
+    if (rank == 0) {
+        int vals[6];
+        MPI_Request req[6];
+        for (int i = 0; i < k; i++) MPI_Irecv(&vals[i], 1, MPI_INT, 1 + i % (size - 1), i, MPI_COMM_WORLD, &req[i]);
+        int done = 0, idx = -1;
+        MPI_Waitany(k, req, &idx, MPI_STATUS_IGNORE);
+        if (idx < 0 || idx >= k) ok = 0;
+        done++;
+        while (done < k) {
+            int out = 0, ids[6];
+            MPI_Waitsome(k, req, &out, ids, MPI_STATUSES_IGNORE);
+            if (out == MPI_UNDEFINED) break;
+            done += out;
+        }
+        int flag = 0;
+        MPI_Testall(k, req, &flag, MPI_STATUSES_IGNORE);
+        if (!flag || done != k) ok = 0;
+        for (int i = 0; i < k; i++)
+            if (vals[i] != 1000 + i) ok = 0;
+    } else {
+        for (int i = 0; i < k; i++)
+            if (1 + i % (size - 1) == rank) {
+                int v = 1000 + i;
+                MPI_Send(&v, 1, MPI_INT, 0, i, MPI_COMM_WORLD);
+            }
+    }
+    return ok;
+}
+
+__device__ int __gpu_main(int argc, char** argv) {
+    int rank, size, ok = 0;
+    MPI_Init(&argc, &argv);
+    MPI_Comm_rank(MPI_COMM_WORLD, &rank);
+    MPI_Comm_size(MPI_COMM_WORLD, &size);
+    const char* s = argc > 1 ? argv[1] : "single_int";
+    if (!strcmp(s, "single_int")) ok = single_int(rank);
+    else if (!strcmp(s, "array16")) ok = array16(rank);
+    else if (!strcmp(s, "sendrecv")) ok = sendrecv(rank);
+    else if (!strcmp(s, "repeat_sizes")) ok = repeat_sizes(rank);
+    else if (!strcmp(s, "flood")) ok = flood(rank, size);
+    else if (!strcmp(s, "all_to_all"))
+        ok = all_to_all(rank, size, argc > 2 ? atoi(argv[2]) : 20, argc > 3 ? atoi(argv[3]) : 0);
+    else if (!strcmp(s, "a2a_ids")) ok = a2a_ids(rank, size, argc > 2 ? atoi(argv[2]) : 3);
+    else if (!strcmp(s, "wildcard")) ok = wildcard(rank, size);
+    else if (!strcmp(s, "probe_order")) ok = probe_order(rank, size);
+    else if (!strcmp(s, "large")) ok = large(rank, size);
+    else if (!strcmp(s, "completion")) ok = completion(rank, size);
+    printf("%s rank %d ok %d\n", s, rank, ok);
+    MPI_Finalize();
+    return 0;
+}
+
+__device__ int __gpu_max_threads() { return 1024; }

@@ -1,0 +1,127 @@
+"""Host collective C ABI (libgpumpi.so) against host folds in rank order."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def coll(gpu_built):
+    import importlib.util
+    import os
+    import sys
+
+    path = os.path.join(gpu_built.PKG, "gpumpi_coll.py")
+    spec = importlib.util.spec_from_file_location("gpumpi_coll", path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod
+    spec.loader.exec_module(mod)
+    lib = gpu_built.load_library()
+    mod.bind(lib)
+    return mod, lib
+
+
+def _rank_fold(xs, op):
+    acc = xs[0].copy()
+    for x in xs[1:]:
+        if op == "sum":
+            acc = x + acc
+        elif op == "max":
+            acc = np.where(x > acc, x, acc)
+        elif op == "min":
+            acc = np.where(x > acc, acc, x)
+        elif op == "prod":
+            acc = x * acc
+    return acc
+
+
+@pytest.mark.parametrize("form", ["plain", "batched", "graph"])
+@pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (32, 1 << 16)])
+def test_capi_collectives(coll, form, nranks, count):
+    import torch
+
+    mod, lib = coll
+    g = torch.Generator().manual_seed(nranks * 1000 + count)
+    comm = mod.Comm(lib, nranks)
+    keep = []
+    descs = []
+    cases = []
+    # allreduce sum fp64 and max int32, bcast, alltoall, allgather, reduce
+    xf = [torch.rand(count, dtype=torch.float64, generator=g) * 2 - 1 for _ in range(nranks)]
+    xi = [torch.randint(-(1 << 20), 1 << 20, (count,), dtype=torch.int32, generator=g) for _ in range(nranks)]
+    df = [t.cuda() for t in xf]
+    di = [t.cuda() for t in xi]
+    of = [torch.empty_like(t) for t in df]
+    oi = [torch.empty_like(t) for t in di]
+    descs.append(mod.make_desc(comm, mod.COLL_ALLREDUCE, "float64", count, [t.data_ptr() for t in df],
+                               [t.data_ptr() for t in of], mod.OP_SUM, 0, keep))
+    descs.append(mod.make_desc(comm, mod.COLL_ALLREDUCE, "int32", count, [t.data_ptr() for t in di],
+                               [t.data_ptr() for t in oi], mod.OP_MAX, 0, keep))
+    root = nranks - 1
+    bb = [t.clone() for t in df]
+    descs.append(mod.make_desc(comm, mod.COLL_BCAST, "float64", count, None, [t.data_ptr() for t in bb],
+                               mod.OP_SUM, root, keep))
+    per = max(1, count // nranks)
+    sa = [torch.randint(0, 1 << 30, (per * nranks,), dtype=torch.int32, generator=g).cuda() for _ in range(nranks)]
+    ra = [torch.empty_like(t) for t in sa]
+    descs.append(mod.make_desc(comm, mod.COLL_ALLTOALL, "int32", per, [t.data_ptr() for t in sa],
+                               [t.data_ptr() for t in ra], 0, 0, keep))
+    ag = [torch.empty(count * nranks, dtype=torch.float64, device="cuda") for _ in range(nranks)]
+    descs.append(mod.make_desc(comm, mod.COLL_ALLGATHER, "float64", count, [t.data_ptr() for t in df],
+                               [t.data_ptr() for t in ag], 0, 0, keep))
+    rd = [torch.zeros(count, dtype=torch.float64, device="cuda") for _ in range(nranks)]
+    descs.append(mod.make_desc(comm, mod.COLL_REDUCE, "float64", count, [t.data_ptr() for t in df],
+                               [t.data_ptr() for t in rd], mod.OP_PROD, 0, keep))
+    plan = mod.Plan(lib, descs, threads=128, batched=(form != "plain"))
+    if form == "graph":
+        plan.capture()
+    for _ in range(2):
+        plan.launch()
+    torch.cuda.synchronize()
+    assert mod.status(lib) is None
+    exp_f = _rank_fold([x.numpy() for x in xf], "sum")
+    exp_i = _rank_fold([x.numpy() for x in xi], "max")
+    exp_p = _rank_fold([x.numpy() for x in xf], "prod")
+    for r in range(nranks):
+        assert np.array_equal(of[r].cpu().numpy().view(np.uint64), exp_f.view(np.uint64))
+        assert np.array_equal(oi[r].cpu().numpy(), exp_i)
+        assert np.array_equal(bb[r].cpu().numpy(), xf[root].numpy())
+        got = ra[r].cpu().numpy()
+        for q in range(nranks):
+            assert np.array_equal(got[q * per:(q + 1) * per], sa[q].cpu().numpy()[r * per:(r + 1) * per])
+        assert np.array_equal(ag[r].cpu().numpy(), np.concatenate([x.numpy() for x in xf]))
+    assert np.array_equal(rd[0].cpu().numpy().view(np.uint64), exp_p.view(np.uint64))
+    plan.close()
+    comm.close()
+
+
+def test_capi_batched_many_comms(coll):
+    """Sixteen communicators of uneven sizes in one persistent launch."""
+    import torch
+
+    mod, lib = coll
+    sizes = [4, 8, 12, 16, 24, 32, 40, 48, 56, 64, 72, 80, 88, 96, 128, 256]
+    count = 4096
+    comms = [mod.Comm(lib, p) for p in sizes]
+    keep, descs, checks = [], [], []
+    g = torch.Generator().manual_seed(7)
+    for c, p in zip(comms, sizes):
+        xs = [torch.randint(-(1 << 20), 1 << 20, (count,), dtype=torch.int32, generator=g) for _ in range(p)]
+        ds = [x.cuda() for x in xs]
+        outs = [torch.empty_like(d) for d in ds]
+        descs.append(mod.make_desc(c, mod.COLL_ALLREDUCE, "int32", count, [d.data_ptr() for d in ds],
+                                   [o.data_ptr() for o in outs], mod.OP_SUM, 0, keep))
+        checks.append((xs, outs, ds))
+    plan = mod.Plan(lib, descs, threads=128, batched=True)
+    plan.capture()
+    plan.launch()
+    plan.launch()
+    torch.cuda.synchronize()
+    assert mod.status(lib) is None
+    for xs, outs, _ in checks:
+        exp = _rank_fold([x.numpy().astype(np.int32) for x in xs], "sum").astype(np.int32)
+        for o in outs:
+            assert np.array_equal(o.cpu().numpy(), exp)
+    plan.close()
+    for c in comms:
+        c.close()
