@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "gpumpi.h"
@@ -560,3 +561,170 @@ extern "C" int gpumpi_api_status(char* msg, int len) {
 }
 
 extern "C" uint64_t gpumpi_kernel_launches(void) { return g_launches; }
+
+// ------------------------------------------------------------------ allocation-free allreduce
+// Some callers may not allocate device memory on their call path: a serving
+// loop that reserved all of HBM when it started, a host thread running under
+// a pooled allocator's fixed budget, or code that must not block the device
+// (cudaMalloc and cudaFree can synchronise it).  gpumpi_allreduce_noalloc
+// serves them: it runs the same allreduce schedule as the plan kernel, but
+// its synchronisation state (communicator tables, flags, per-rank handles,
+// error words) lives in the fixed array below instead of cudaMalloc'd memory.
+//
+// The array is a file-scope device variable, so every GPU that loads this
+// library holds it until the process exits, and every call shares it: each
+// call rewrites the part it uses (clearing the flags), and calls whose
+// kernels overlap on the GPU race on it.  Host code may not use the array's
+// name as a device address; the entry point looks the address up with
+// cudaGetSymbolAddress the first time it runs on a device (with that device
+// current), so that first call should come before any stream capture.
+namespace {
+
+constexpr int NOALLOC_MAX_RANKS = 256;
+constexpr size_t NOALLOC_SCRATCH_BYTES = 64 * 1024;
+
+static __device__ __align__(256) unsigned char gm_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+struct NoallocLayout {
+    size_t job, status, err, cs, pub, flags, handles, dcomm, desc, first, ptrs, total;
+};
+
+NoallocLayout noalloc_layout(int n) {
+    NoallocLayout L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        o = (o + 255) & ~(size_t)255;
+        size_t at = o;
+        o += bytes;
+        return at;
+    };
+    L.job = take(sizeof(Job));
+    L.status = take(sizeof(int) * 16);
+    L.err = take(256);
+    L.cs = take(sizeof(CommShared));
+    L.pub = take(sizeof(Pub) * n);
+    L.flags = take(sizeof(u64) * 3 * n);
+    L.handles = take(sizeof(MPI_Comm_impl) * n);
+    L.dcomm = take(sizeof(DevComm));
+    L.desc = take(sizeof(DevDesc));
+    L.first = take(sizeof(int) * 2);
+    L.ptrs = take(sizeof(void*) * 2 * n);
+    L.total = take(0);
+    return L;
+}
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_dev_ptr[64];                                    // per device, looked up once
+unsigned char g_noalloc_image[NOALLOC_SCRATCH_BYTES];           // host image of the used prefix
+
+}  // namespace
+
+// See include/gpumpi.h.  Synchronises `stream`; returns 0 or an error code.
+extern "C" int gpumpi_allreduce_noalloc(void* const* sendbufs, void* const* recvbufs, int nranks,
+                                        uint64_t count, int dtype, int redop, int threads_per_rank,
+                                        void* stream) {
+    if (nranks < 1 || nranks > NOALLOC_MAX_RANKS) {
+        char m[160];
+        snprintf(m, sizeof(m), "gpumpi_allreduce_noalloc: %d ranks requested, the fixed scratch holds at most %d",
+                 nranks, NOALLOC_MAX_RANKS);
+        set_last_error(m);
+        return GPUMPI_EINVAL;
+    }
+    const int es = esize_of(dtype);
+    if (!sendbufs || !recvbufs || es < 0 || redop < 0 || redop > 3) {
+        set_last_error("gpumpi_allreduce_noalloc: bad buffers, datatype or operator");
+        return GPUMPI_EINVAL;
+    }
+    if (threads_per_rank == 0) threads_per_rank = 128;
+    if (threads_per_rank < 64 || threads_per_rank > 1024 || threads_per_rank % 32) return GPUMPI_EINVAL;
+    for (int r = 0; r < nranks; r++)
+        if (!sendbufs[r] || !recvbufs[r]) return GPUMPI_EINVAL;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return GPUMPI_EINVAL;
+    if (!g_noalloc_dev_ptr[dev]) {
+        void* p = nullptr;
+        CK(cudaGetSymbolAddress(&p, gm_noalloc_scratch));
+        g_noalloc_dev_ptr[dev] = p;
+    }
+    char* base = (char*)g_noalloc_dev_ptr[dev];
+    const NoallocLayout L = noalloc_layout(nranks);
+    const size_t smem = sizeof(BlockCtx) + 64;
+    int per = 0, sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)gpumpi_plan_kernel, threads_per_rank, smem));
+    if ((long long)per * sms < nranks) {
+        set_last_error("gpumpi_allreduce_noalloc: rank blocks cannot all be resident");
+        return GPUMPI_ENORES;
+    }
+    // Build the used prefix on the host (zeros clear the flags), then copy it.
+    unsigned char* img = g_noalloc_image;
+    memset(img, 0, L.total);
+    Job& job = *(Job*)(img + L.job);
+    job.id = -2;
+    job.timeout_ns = 30ull * 1000000000ull;
+    job.status = (int*)(base + L.status);
+    job.err_msg = base + L.err;
+    CommShared& cs = *(CommShared*)(img + L.cs);
+    cs.size = nranks;
+    cs.ctx = 1;
+    cs.members = nullptr;
+    cs.pub = (Pub*)(base + L.pub);
+    cs.arrive = (u64*)(base + L.flags);
+    cs.mid = cs.arrive + nranks;
+    cs.depart = cs.arrive + 2 * (size_t)nranks;
+    MPI_Comm_impl* h = (MPI_Comm_impl*)(img + L.handles);
+    for (int r = 0; r < nranks; r++) {
+        h[r].kind = 1;
+        h[r].ctx = 1;
+        h[r].size = nranks;
+        h[r].rank = r;
+        h[r].refcnt = 1;
+        h[r].cs = (CommShared*)(base + L.cs);
+        h[r].seq = 0;
+    }
+    DevComm& dc = *(DevComm*)(img + L.dcomm);
+    dc.handles = (MPI_Comm_impl*)(base + L.handles);
+    dc.size = nranks;
+    void** ptrs = (void**)(img + L.ptrs);
+    for (int r = 0; r < nranks; r++) {
+        ptrs[r] = sendbufs[r];
+        ptrs[nranks + r] = recvbufs[r];
+    }
+    DevDesc& d = *(DevDesc*)(img + L.desc);
+    d.op = GPUMPI_COLL_ALLREDUCE;
+    d.dtype = dtype;
+    d.redop = redop;
+    d.root = 0;
+    d.count = count;
+    d.comm = 0;
+    d.esize = es;
+    d.algo = 0;
+    d.sbufs = (void**)(base + L.ptrs);
+    d.rbufs = (void**)(base + L.ptrs) + nranks;
+    int* first = (int*)(img + L.first);
+    first[0] = 0;
+    first[1] = 1;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(base, img, L.total, cudaMemcpyHostToDevice, st));
+    PlanArgs args;
+    args.job = (Job*)(base + L.job);
+    args.descs = (const DevDesc*)(base + L.desc);
+    args.comm_first = (const int*)(base + L.first);
+    args.slot_comm = nullptr;
+    args.slot_rank = nullptr;
+    args.comms = (const DevComm*)(base + L.dcomm);
+    int rc = launch((const void*)gpumpi_plan_kernel, nranks, threads_per_rank, smem, &args, st);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(st));
+    int status[16];
+    CK(cudaMemcpy(status, base + L.status, sizeof(status), cudaMemcpyDeviceToHost));
+    if (status[1] != 0) {
+        char m[160];
+        snprintf(m, sizeof(m), "gpumpi_allreduce_noalloc: device error %d on rank %d", status[1], status[2]);
+        set_last_error(m);
+        return GPUMPI_EJOB;
+    }
+    return GPUMPI_OK;
+}

@@ -149,6 +149,23 @@ int gpumpi_plan_destroy(gpumpi_plan_t plan);
  * returns GPUMPI_EJOB and clears it when an error was recorded. */
 int gpumpi_api_status(char* msg, int len);
 
+/* Allreduce over nranks device buffers that allocates no device memory.
+ * No counterpart in the reference (it had no host-side collective API).
+ * For callers that may not allocate on their call path -- a server that
+ * reserved all of HBM at start-up, code under a fixed pooled-allocator
+ * budget, or a thread that must not let cudaMalloc/cudaFree synchronise the
+ * device.  The runtime's synchronisation state lives in a fixed 64 KiB array
+ * in device memory, so nranks is limited to 256 (larger requests fail with
+ * GPUMPI_EINVAL).  sendbufs/recvbufs are host arrays of nranks device
+ * pointers; count elements of dtype are reduced with redop in rank order.
+ * The first call on a device looks up the array's address (with that device
+ * current) and should therefore come before any stream capture.  All calls
+ * share the array: calls whose kernels overlap on the GPU race.  The call
+ * synchronises `stream` and returns 0 or an error code. */
+int gpumpi_allreduce_noalloc(void* const* sendbufs, void* const* recvbufs, int nranks,
+                             uint64_t count, int dtype, int redop, int threads_per_rank,
+                             void* stream);
+
 /* Number of kernel launches this process issued through the collective API. */
 uint64_t gpumpi_kernel_launches(void);
 
