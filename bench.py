@@ -63,9 +63,13 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5 and self.proc.poll() is None:
+                time.sleep(0.01)      # the timed region starts once sampling runs
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -104,6 +108,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes (read + write) of one batched launch at 2^15 elements per rank,
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); the
+# traffic grows in proportion with the per-rank count and is scaled by it.
+NCU_TRAFFIC_BYTES_2_15 = 0.932655616e9 + 1.469682e9
+
+
 def alg_bytes(sizes, n):
     total = 0
     for p in sizes:
@@ -113,6 +123,15 @@ def alg_bytes(sizes, n):
             per = n // p
             total += 2 * p * p * per * s    # Alltoall
     return total
+
+
+def max_over_ranks(dist, torch, secs: float) -> float:
+    """Replicas: the job's time is the slowest rank's (gloo all-reduce MAX)."""
+    if dist is None:
+        return secs
+    t = torch.tensor([secs], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1):
@@ -172,33 +191,31 @@ def run_oracle_bench(lg: int, iters: int, ranks: int = 1024, timeout: float = 90
 
 
 def reference_arm(args):
+    """The same collectives through the hostmpi oracle on the host cores.
+
+    One warm-up invocation of W iterations, then one invocation that runs and
+    times K iterations (the program's own MPI_Wtime around its loop), so that
+    the 1024 processes start twice, not once per step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    lg, iters = args.cpu_lg, args.cpu_iters
-    vals = []
-    for _ in range(args.warmup):
-        run_oracle_bench(lg, 1)
-    t0 = time.time()
-    for _ in range(args.steps):
-        gbps, secs, nbytes = run_oracle_bench(lg, iters)
-        vals.append(gbps)
-    wall = time.time() - t0
-    value = sum(vals) / len(vals)
+    lg = args.cpu_lg
+    run_oracle_bench(lg, args.warmup)
+    gbps, secs, nbytes = run_oracle_bench(lg, args.steps)
     cores = os.cpu_count()
     sample = (f"1024 host processes (hostmpi), the same 16 communicators and six collectives, "
-              f"2^{lg} elements per rank, {iters} iteration(s) per step")
+              f"2^{lg} elements per rank, {args.steps} timed iterations")
     line = {
         "impl": "reference", "metric": "collective GB/s (batched collectives, algorithmic bytes)",
-        "value": round(value, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(1000 * wall / max(1, args.steps), 3),
+        "value": round(gbps, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * secs / max(1, args.steps), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
         "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "elements_per_rank": 1 << lg, "comm_sizes": COMM_SIZES,
-                   "l2": "inputs larger than L2 not applicable (host memory)"},
-        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                   "l2": "host memory (not applicable)"},
+        "cpu_baseline": {"value": round(gbps, 3), "unit": "GB/s", "cores": cores, "kind": "port",
                          "sample": sample},
-        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": round(gbps, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -206,7 +223,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--lg", type=int, default=20, help="log2 elements per rank")
@@ -258,10 +275,7 @@ def main():
     err = coll.status(lib)
     if err:
         raise SystemExit(f"device error during benchmark: {err}")
-    if dist:
-        t = torch.tensor([secs], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
+    secs = max_over_ranks(dist, torch, secs)
     nbytes = alg_bytes(COMM_SIZES, n)
     per_step = secs / args.steps
     value = nbytes * args.steps * world / secs / 1e9
@@ -342,7 +356,11 @@ def main():
             "plain": {"value": round(plain_gbs, 2), "unit": "GB/s", "launches_per_step": len(descs),
                       "batched_over_plain": round(value / world / plain_gbs, 2)},
             "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind, "traffic": None},
+                         "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind,
+                         "traffic": int(NCU_TRAFFIC_BYTES_2_15 * n / (1 << 15)),
+                         "traffic_note": "bytes per launch, ncu DRAM read+write at 2^15 elements per rank "
+                                         "scaled by elements per rank",
+                         "algorithmic_bytes": int(nbytes)},
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne},
             "cpu_baseline": cpu,

@@ -13,11 +13,7 @@ using namespace gm;
 
 namespace gm {
 
-__device__ int aborted_code() {
-    Job* j = bctx().job;
-    int code = ld_acquire_int(&j->status[1]);
-    return code ? code : GPUMPI_ERR_ABORTED;
-}
+__device__ int aborted_code() { return fail_code(bctx().job); }
 
 __device__ MPI_Request_impl* req_alloc() {
     RankPriv* p = bctx().priv;

@@ -212,7 +212,8 @@ static GM_HD void pad_out(Sink& o, const Spec& sp, const char* sign, int nsign, 
 
 // Significant digits with decimal exponent: value = 0.d1d2... * 10^(E+1).
 // Produces `nsig` rounded significant digits into sig and returns E.
-static GM_HD GM_NOINLINE int sig_digits(double v, int nsig, char* sig) {
+static GM_HD GM_NOINLINE int sig_digits(double v, int nsig, char* sig, bool* carried = nullptr) {
+    if (carried) *carried = false;
     Digits dg;
     dg.init(v);
     int E;
@@ -255,6 +256,7 @@ static GM_HD GM_NOINLINE int sig_digits(double v, int nsig, char* sig) {
             sig[0] = '1';
             for (int i = 1; i < nsig; i++) sig[i] = '0';
             E++;
+            if (carried) *carried = true;
         }
     }
     return E;
@@ -346,12 +348,18 @@ static GM_HD GM_NOINLINE void fmt_float(Sink& o, Spec sp, double v) {
         int P = prec == 0 ? 1 : prec;
         char sig[720];
         int E = 0;
+        bool carried = false;
         if (a == 0.0) {
             for (int i = 0; i < P; i++) sig[i] = '0';
             E = 0;
         } else {
-            E = sig_digits(a, P, sig);
+            E = sig_digits(a, P, sig, &carried);
         }
+        // glibc picks the style from the exponent before rounding: a value
+        // just below 10^P that rounds up to it was set for fixed style with no
+        // fraction digits, and glibc keeps that digit count when it switches
+        // to exponent style ("%#.2g" of 99.96 prints "1.e+02").
+        const bool glibc_carry = sp.alt && carried && E == P;
         int nsig = P;
         if (!sp.alt)
             while (nsig > 1 && sig[nsig - 1] == '0') nsig--;
@@ -371,7 +379,7 @@ static GM_HD GM_NOINLINE void fmt_float(Sink& o, Spec sp, double v) {
             }
         } else {
             body[nb++] = sig[0];
-            int nf = sp.alt ? P - 1 : nsig - 1;
+            int nf = glibc_carry ? 0 : sp.alt ? P - 1 : nsig - 1;
             if (nf > 0 || sp.alt) body[nb++] = '.';
             for (int i = 1; i <= nf; i++) body[nb++] = sig[i];
             nb += fmt_exp(body + nb, E, upper);

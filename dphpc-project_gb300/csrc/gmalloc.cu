@@ -6,9 +6,16 @@
 // lanes of a warp ask for the same class at once, the lowest lane claims a
 // batch of bits for all of them in one atomic and hands them out (warp
 // aggregation).  Free clears the bit with atomicAnd; a chunk's page and class
-// follow from its address.  Requests above 32 KiB take whole pages: exact-size
-// runs of fewer than 64 pages are recycled through tagged (ABA-safe) stacks,
-// longer runs come from the bump pointer and are not recycled.
+// follow from its address.  A claim scans a window of the class's pages from
+// a per-SM-stripe hint; freed chunks outside that window are found through a
+// per-class tagged (ABA-safe) stack of pages that have free chunks, onto which
+// a free pushes its page unless it is already listed; only when both come up
+// empty does a claim take a fresh page.  Requests above 32 KiB take runs of
+// whole pages from one address-ordered list of free runs (first fit, split on
+// allocation, merged with both neighbours on free) or, when no run fits, from
+// the bump pointer.  The list sits behind a lock whose wait is bounded by the
+// global timer (a wait that runs out returns NULL); large requests are rare,
+// so the lock is not a hot spot.
 //
 // This replaces CUDA's device malloc (gpu_libs/gpu_libc/stdlib.cu:70-91) and
 // the reference's experimental coalescing allocators (gpu_libs/gpu_malloc/*),
@@ -21,18 +28,55 @@ namespace gm {
 constexpr u32 PAGE = 64 * 1024;
 constexpr int NCLS = 12;
 constexpr int HINTS = 32;
-constexpr int LARGE_BUCKETS = 64;
-constexpr u32 CLS_LARGE = 0xFE;
+constexpr u32 CLS_LARGE = 0xFE;       // first page of an allocated large run
+constexpr u32 CLS_FREE_RUN = 0xFD;    // first page of a free large run
+constexpr u64 LOCK_WAIT_NS = 2000000000ull;
 constexpr u32 NO_PAGE = 0xffffffffu;
 constexpr int SCAN_PAGES = 64;
 
 struct PageMeta {
     u32 cls;
-    u32 npages;
-    u32 next;       // large free-list link: page + 1, 0 = end
-    u32 pad;
+    u32 npages;     // pages of a large run (first page only)
+    u32 next;       // free-run list link: page + 1, 0 = end
+    u32 slot;       // index of the page in its class list
+    u32 pnext;      // partial-stack link: page + 1, 0 = end
+    u32 listed;     // 1 while the page is on its class's partial stack
     u64 bits[64];
 };
+static_assert(sizeof(PageMeta) % 8 == 0 && offsetof(PageMeta, bits) % 8 == 0, "64-bit atomics on bits");
+
+// Partial-page stacks: heads hold (tag << 32) | (page + 1).
+static __device__ void push_partial(Heap* h, int c, u32 p) {
+    PageMeta* pm = &h->meta[p];
+    if (atomicCAS(&pm->listed, 0u, 1u) != 0u) return;
+    u64* head = &h->partial[c];
+    u64 old = *(volatile u64*)head;
+    for (;;) {
+        *(volatile u32*)&pm->pnext = (u32)(old & 0xffffffffull);
+        __threadfence();
+        const u64 nw = (((old >> 32) + 1) << 32) | (u64)(p + 1);
+        const u64 seen = atomicCAS(head, old, nw);
+        if (seen == old) return;
+        old = seen;
+    }
+}
+
+static __device__ u32 pop_partial(Heap* h, int c) {
+    u64* head = &h->partial[c];
+    u64 old = *(volatile u64*)head;
+    while ((old & 0xffffffffull) != 0) {
+        const u32 cand = (u32)(old & 0xffffffffull) - 1;
+        const u32 nxt = *(volatile u32*)&h->meta[cand].pnext;
+        const u64 nw = (((old >> 32) + 1) << 32) | nxt;
+        const u64 seen = atomicCAS(head, old, nw);
+        if (seen == old) {
+            atomicExch(&h->meta[cand].listed, 0u);
+            return cand;
+        }
+        old = seen;
+    }
+    return 0xffffffffu;
+}
 
 static __device__ __forceinline__ int class_of(u64 bytes) {
     if (bytes <= 16) return 0;
@@ -116,17 +160,35 @@ static __device__ bool claim_batch(Heap* h, int c, int want, u32* page, int* w, 
             }
         }
     }
-    // Fresh page from the bump pointer; its bitmap is still all zero.
+    // Pages whose chunks were freed outside the window.
+    for (int tries = 0; tries < 16; tries++) {
+        const u32 p = pop_partial(h, c);
+        if (p == NO_PAGE) break;
+        if (claim_in_page(h, p, c, want, (int)(stripe % words_of(c)), w, m)) {
+            *hint = *(volatile u32*)&h->meta[p].slot;   // the window moves to a page with room
+            *page = p;
+            return true;
+        }
+    }
+    // Fresh page from the bump pointer; its bitmap is still all zero.  Claim
+    // this group's chunks before the page is published in the class list:
+    // once listed, other warps may take its chunks, and a page of a large
+    // class (16 or 32 chunks) could be drained before its creator claimed any.
+    // (checked first, so a full heap does not keep moving the bump pointer:
+    // it overshoots npages by at most the number of concurrent claimers)
+    if (*(volatile u32*)h->next_page >= h->npages) return false;
     u32 p = atomicAdd(h->next_page, 1u);
     if (p >= h->npages) return false;
     h->meta[p].cls = (u32)c;
+    if (!claim_in_page(h, p, c, want, 0, w, m)) return false;
     __threadfence();
     u32 slot = atomicAdd(&h->cls_count[c], 1u);
+    h->meta[p].slot = slot;
+    __threadfence();
     if (slot < h->npages) {
         ((volatile u32*)h->cls_pages)[(u64)c * h->npages + slot] = p;
         *hint = slot;
     }
-    if (!claim_in_page(h, p, c, want, 0, w, m)) return false;
     *page = p;
     return true;
 }
@@ -163,35 +225,104 @@ static __device__ void* small_alloc(Heap* h, int c) {
     return result;
 }
 
+static __device__ bool large_lock(Heap* h) {
+    if (atomicCAS(h->large_lock, 0u, 1u) != 0u) {
+        const u64 t0 = gtime();
+        while (atomicCAS(h->large_lock, 0u, 1u) != 0u) {
+            if (gtime() - t0 > LOCK_WAIT_NS) {
+                atomicAdd(&h->stats[2], 1u);
+                return false;
+            }
+            __nanosleep(64);
+        }
+    }
+    __threadfence();
+    return true;
+}
+
+static __device__ void large_unlock(Heap* h) {
+    __threadfence();
+    atomicExch(h->large_lock, 0u);
+}
+
 static __device__ void* large_alloc(Heap* h, u64 bytes) {
     const u64 n64 = (bytes + PAGE - 1) / PAGE;
     if (n64 > h->npages) return nullptr;
     const u32 n = (u32)n64;
+    if (!large_lock(h)) return nullptr;
+    volatile PageMeta* meta = h->meta;
     u32 p = NO_PAGE;
-    if (n < LARGE_BUCKETS) {
-        u64* head = &h->large_free[n];
-        u64 old = *(volatile u64*)head;
-        while ((old & 0xffffffffull) != 0) {
-            u32 cand = (u32)(old & 0xffffffffull) - 1;
-            u32 nxt = *(volatile u32*)&h->meta[cand].next;
-            u64 nw = (((old >> 32) + 1) << 32) | nxt;
-            u64 seen = atomicCAS(head, old, nw);
-            if (seen == old) {
-                p = cand;
+    u32 prev = NO_PAGE;
+    u32 cur = *(volatile u32*)h->large_head;   // page + 1
+    while (cur) {
+        const u32 c = cur - 1;
+        const u32 len = meta[c].npages;
+        const u32 nxt = meta[c].next;
+        if (len >= n) {
+            u32 link = nxt;
+            if (len > n) {                   // split: the tail stays free
+                const u32 rest = c + n;
+                meta[rest].cls = CLS_FREE_RUN;
+                meta[rest].npages = len - n;
+                meta[rest].next = nxt;
+                link = rest + 1;
+            }
+            if (prev == NO_PAGE) *(volatile u32*)h->large_head = link;
+            else meta[prev].next = link;
+            p = c;
+            break;
+        }
+        prev = c;
+        cur = nxt;
+    }
+    if (p == NO_PAGE) {   // bump pointer, only when the run fits (a failed request moves nothing)
+        u32 first = *(volatile u32*)h->next_page;
+        while ((u64)first + n <= h->npages) {
+            const u32 seen = atomicCAS(h->next_page, first, first + n);
+            if (seen == first) {
+                p = first;
                 break;
             }
-            old = seen;
+            first = seen;
         }
     }
-    if (p == NO_PAGE) {
-        u32 first = atomicAdd(h->next_page, n);
-        if ((u64)first + n > h->npages) return nullptr;
-        p = first;
+    if (p != NO_PAGE) {
+        meta[p].cls = CLS_LARGE;
+        meta[p].npages = n;
     }
-    h->meta[p].cls = CLS_LARGE;
-    h->meta[p].npages = n;
-    __threadfence();
-    return h->base + (u64)p * PAGE;
+    large_unlock(h);
+    return p == NO_PAGE ? nullptr : h->base + (u64)p * PAGE;
+}
+
+// Return a large run to the free list, merged with free neighbours.
+static __device__ void large_release(Heap* h, u32 p) {
+    if (!large_lock(h)) return;               // counted in stats[2]; the run is lost
+    volatile PageMeta* meta = h->meta;
+    u32 n = meta[p].npages;
+    u32 prev = NO_PAGE;
+    u32 cur = *(volatile u32*)h->large_head;
+    while (cur && cur - 1 < p) {
+        prev = cur - 1;
+        cur = meta[prev].next;
+    }
+    u32 link = cur;
+    if (cur && p + n == cur - 1) {            // merge with the next free run
+        n += meta[cur - 1].npages;
+        link = meta[cur - 1].next;
+        meta[cur - 1].cls = 0;
+    }
+    if (prev != NO_PAGE && prev + meta[prev].npages == p) {   // merge into the previous run
+        meta[prev].npages = meta[prev].npages + n;
+        meta[prev].next = link;
+        meta[p].cls = 0;
+    } else {
+        meta[p].cls = CLS_FREE_RUN;
+        meta[p].npages = n;
+        meta[p].next = link;
+        if (prev == NO_PAGE) *(volatile u32*)h->large_head = p + 1;
+        else meta[prev].next = p + 1;
+    }
+    large_unlock(h);
 }
 
 __device__ void* heap_alloc(Heap* h, u64 bytes) {
@@ -217,21 +348,15 @@ __device__ void heap_free(Heap* h, void* ptr) {
         const u64 chunk = (off % PAGE) >> (4 + cls);
         __threadfence();
         atomicAnd(&pm->bits[chunk / 64], ~(1ull << (chunk % 64)));
+        if (*(volatile u32*)&pm->listed == 0u) push_partial(h, (int)cls, p);
         return;
     }
     if (cls == CLS_LARGE) {
-        const u32 n = pm->npages;
-        if (n >= LARGE_BUCKETS || (off % PAGE) != 0) return;
-        u64* head = &h->large_free[n];
-        u64 old = *(volatile u64*)head;
-        for (;;) {
-            pm->next = (u32)(old & 0xffffffffull);
-            __threadfence();
-            u64 nw = (((old >> 32) + 1) << 32) | (u64)(p + 1);
-            u64 seen = atomicCAS(head, old, nw);
-            if (seen == old) break;
-            old = seen;
+        if ((off % PAGE) != 0) {
+            atomicAdd(&h->stats[1], 1u);
+            return;
         }
+        large_release(h, p);
         return;
     }
     atomicAdd(&h->stats[1], 1u);
@@ -245,6 +370,31 @@ __device__ u64 heap_usable_size(Heap* h, void* ptr) {
     if (pm->cls < NCLS) return 16ull << pm->cls;
     if (pm->cls == CLS_LARGE) return (u64)pm->npages * PAGE;
     return 0;
+}
+
+// Control words of a heap, in one zero-initialised block: the tagged heads of
+// the partial-page stacks, the class page counts, the per-stripe hints, the
+// bump pointer, the free-run list head and lock, and the statistics
+// (0 small allocations, 1 frees of foreign pointers, 2 lock waits that ran out).
+constexpr size_t CTL_PARTIAL = 0;
+constexpr size_t CTL_COUNT = CTL_PARTIAL + sizeof(u64) * NCLS;
+constexpr size_t CTL_HINT = CTL_COUNT + sizeof(u32) * NCLS;
+constexpr size_t CTL_NEXT = CTL_HINT + sizeof(u32) * NCLS * HINTS;
+constexpr size_t CTL_LARGE_HEAD = CTL_NEXT + sizeof(u32);
+constexpr size_t CTL_LARGE_LOCK = CTL_LARGE_HEAD + sizeof(u32);
+constexpr size_t CTL_STATS = CTL_LARGE_LOCK + sizeof(u32);
+constexpr size_t CTL_BYTES = (CTL_STATS + sizeof(u32) * 8 + 255) & ~(size_t)255;
+
+__host__ size_t heap_ctl_bytes() { return CTL_BYTES; }
+
+__host__ void heap_set_ctl(Heap& h, char* ctl) {
+    h.large_head = (u32*)(ctl + CTL_LARGE_HEAD);
+    h.large_lock = (u32*)(ctl + CTL_LARGE_LOCK);
+    h.partial = (u64*)(ctl + CTL_PARTIAL);
+    h.cls_count = (u32*)(ctl + CTL_COUNT);
+    h.cls_hint = (u32*)(ctl + CTL_HINT);
+    h.next_page = (u32*)(ctl + CTL_NEXT);
+    h.stats = (u32*)(ctl + CTL_STATS);
 }
 
 }  // namespace gm

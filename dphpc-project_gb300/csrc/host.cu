@@ -85,7 +85,7 @@ size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, cha
     size_t o_status = c.take(sizeof(int) * 16);
     size_t o_ret = c.take(sizeof(int) * (size_t)n);
     size_t o_offs = c.take(sizeof(u64) * 4);
-    size_t o_hctl = c.take(sizeof(u32) * (12 + 12 * 32 + 1 + 8) + sizeof(u64) * 64);
+    size_t o_hctl = c.take(heap_ctl_bytes());
     size_t o_meta = c.take(meta_bytes * npages);
     size_t o_arena = c.take(((size_t)4 << 20) + (size_t)n * 4096);
     size_t arena_bytes = ((size_t)4 << 20) + (size_t)n * 4096;
@@ -146,12 +146,7 @@ size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, cha
     h.bytes = (u64)npages * 65536;
     h.npages = npages;
     h.meta = (PageMeta*)(base + o_meta);
-    u32* hc = (u32*)(base + o_hctl);
-    h.cls_count = hc;
-    h.cls_hint = hc + 12;
-    h.next_page = hc + 12 + 12 * 32;
-    h.stats = hc + 12 + 12 * 32 + 1;
-    h.large_free = (u64*)(((uintptr_t)(hc + 12 + 12 * 32 + 1 + 8) + 7) & ~(uintptr_t)7);
+    heap_set_ctl(h, base + o_hctl);
     h.cls_pages = (u32*)(base + o_clsp);
     // communicator tables (host copies, uploaded by the caller)
     hj.world.size = n;
@@ -324,6 +319,77 @@ int choose_threads(const void* kernel, int n, int requested, size_t smem, int* m
 
 }  // namespace gm
 
+namespace gm {
+
+// Device image of argv: the pointer table, then the strings, with the
+// pointers relocated to where the image will sit in device memory.
+size_t argv_image_bytes(int argc, char** argv) {
+    size_t n = sizeof(char*) * (argc + 1) + 16;
+    for (int i = 0; i < argc; i++) n += strlen(argv[i]) + 1;
+    return (n + 15) & ~(size_t)15;
+}
+
+void argv_image(int argc, char** argv, char* dev, std::vector<char>& img) {
+    img.assign(argv_image_bytes(argc, argv), 0);
+    char** ptrs = (char**)img.data();
+    char* s = img.data() + sizeof(char*) * (argc + 1);
+    for (int i = 0; i < argc; i++) {
+        size_t l = strlen(argv[i]) + 1;
+        memcpy(s, argv[i], l);
+        ptrs[i] = dev + (s - img.data());
+        s += l;
+    }
+    ptrs[argc] = nullptr;
+}
+
+// Copy a finished job's status, return values and output text back and
+// derive its exit status (0 when every rank returned 0 and nothing failed).
+int job_collect(HostJob& hj, cudaStream_t st, JobResult& r) {
+    Job& j = hj.job;
+    const int n = hj.nranks;
+    u64 offs[4];
+    char errmsg[256];
+    r.rets.assign(n, 0);
+    HCHECK(cudaMemcpyAsync(r.status, j.status, sizeof(r.status), cudaMemcpyDeviceToHost, st));
+    HCHECK(cudaMemcpyAsync(offs, j.out_off, sizeof(offs), cudaMemcpyDeviceToHost, st));
+    HCHECK(cudaMemcpyAsync(r.rets.data(), j.retvals, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    HCHECK(cudaMemcpyAsync(errmsg, j.err_msg, sizeof(errmsg), cudaMemcpyDeviceToHost, st));
+    HCHECK(cudaStreamSynchronize(st));
+    errmsg[255] = 0;
+    r.errmsg = errmsg;
+    const size_t nout = offs[0] < j.out_bytes ? offs[0] : j.out_bytes;
+    const size_t nerr = offs[1] < j.out_bytes ? offs[1] : j.out_bytes;
+    r.out.assign(nout, 0);
+    r.err.assign(nerr, 0);
+    if (nout) HCHECK(cudaMemcpyAsync(&r.out[0], j.out, nout, cudaMemcpyDeviceToHost, st));
+    if (nerr) HCHECK(cudaMemcpyAsync(&r.err[0], j.errout, nerr, cudaMemcpyDeviceToHost, st));
+    HCHECK(cudaStreamSynchronize(st));
+    r.truncated = offs[0] > j.out_bytes || offs[1] > j.out_bytes;
+    r.exit_code = 0;
+    r.diag.clear();
+    if (r.truncated) r.diag += "GPUMPI: output truncated (raise --out-bytes)\n";
+    if (r.status[1] != 0) {
+        char m[400];
+        snprintf(m, sizeof(m), "job failed: error %d on rank %d: %s", r.status[1], r.status[2], errmsg);
+        set_last_error(m);
+        r.diag += std::string("GPUMPI: ") + m + "\n";
+        r.exit_code = 1;
+    }
+    if (r.status[3] != n) {
+        char m[120];
+        snprintf(m, sizeof(m), "GPUMPI: only %d of %d ranks finished\n", r.status[3], n);
+        r.diag += m;
+        r.exit_code = 1;
+    }
+    for (int q = 0; q < n; q++)
+        if (r.rets[q] != 0) r.exit_code = 1;
+    return GPUMPI_OK;
+}
+
+double now_seconds() { return now_s(); }
+
+}  // namespace gm
+
 extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog_argv,
                                   const gpumpi_opts* in_opts) {
     gpumpi_opts o = *in_opts;
@@ -356,22 +422,10 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     host_job_layout(hj, o, n, 0, base);
 
     // argv in device memory
-    size_t strbytes = 0;
-    for (int i = 0; i < prog_argc; i++) strbytes += strlen(prog_argv[i]) + 1;
-    std::vector<char> hargs(sizeof(char*) * (prog_argc + 1) + strbytes + 16);
+    std::vector<char> hargs;
     char* dargs = nullptr;
-    HCHECK(cudaMalloc(&dargs, hargs.size()));
-    {
-        char** ptrs = (char**)hargs.data();
-        char* s = hargs.data() + sizeof(char*) * (prog_argc + 1);
-        for (int i = 0; i < prog_argc; i++) {
-            size_t l = strlen(prog_argv[i]) + 1;
-            memcpy(s, prog_argv[i], l);
-            ptrs[i] = dargs + (s - hargs.data());
-            s += l;
-        }
-        ptrs[prog_argc] = nullptr;
-    }
+    HCHECK(cudaMalloc(&dargs, argv_image_bytes(prog_argc, prog_argv)));
+    argv_image(prog_argc, prog_argv, dargs, hargs);
     hj.job.argc = prog_argc;
     hj.job.argv = (char**)dargs;
     hj.job.threads = T;
@@ -398,6 +452,7 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     L.nslots = n;
     L.slot_job = dslots;
     L.slot_rank = dslots + n;
+    L.slot_base = 0;
     void* args[] = {&L};
     if (o.verbose)
         fprintf(stderr, "GPUMPI: %d ranks x %d threads, job memory %.1f MiB, heap %.1f MiB\n", n, T,
@@ -423,45 +478,13 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     }
     HCHECK(cudaStreamSynchronize(st));
 
-    // results
-    Job& j = hj.job;
-    int status[16];
-    u64 offs[4];
-    std::vector<int> rets(n);
-    char errmsg[256];
-    HCHECK(cudaMemcpy(status, j.status, sizeof(status), cudaMemcpyDeviceToHost));
-    HCHECK(cudaMemcpy(offs, j.out_off, sizeof(offs), cudaMemcpyDeviceToHost));
-    HCHECK(cudaMemcpy(rets.data(), j.retvals, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    HCHECK(cudaMemcpy(errmsg, j.err_msg, sizeof(errmsg), cudaMemcpyDeviceToHost));
-    errmsg[255] = 0;
-    size_t nout = offs[0] < j.out_bytes ? offs[0] : j.out_bytes;
-    size_t nerr = offs[1] < j.out_bytes ? offs[1] : j.out_bytes;
-    std::vector<char> text(nout > nerr ? nout : nerr);
-    if (nout) {
-        HCHECK(cudaMemcpy(text.data(), j.out, nout, cudaMemcpyDeviceToHost));
-        fwrite(text.data(), 1, nout, stdout);
-    }
+    JobResult res;
+    rc = job_collect(hj, st, res);
+    if (rc) return rc;
+    fwrite(res.out.data(), 1, res.out.size(), stdout);
     fflush(stdout);
-    if (nerr) {
-        HCHECK(cudaMemcpy(text.data(), j.errout, nerr, cudaMemcpyDeviceToHost));
-        fwrite(text.data(), 1, nerr, stderr);
-    }
-    if (offs[0] > j.out_bytes || offs[1] > j.out_bytes)
-        fprintf(stderr, "GPUMPI: output truncated (raise --out-bytes)\n");
-    int exit_code = 0;
-    if (status[1] != 0) {
-        char m[400];
-        snprintf(m, sizeof(m), "job failed: error %d on rank %d: %s", status[1], status[2], errmsg);
-        set_last_error(m);
-        fprintf(stderr, "GPUMPI: %s\n", m);
-        exit_code = 1;
-    }
-    if (status[3] != n) {
-        fprintf(stderr, "GPUMPI: only %d of %d ranks finished\n", status[3], n);
-        exit_code = 1;
-    }
-    for (int r = 0; r < n; r++)
-        if (rets[r] != 0) exit_code = 1;
+    fwrite(res.err.data(), 1, res.err.size(), stderr);
+    fputs(res.diag.c_str(), stderr);
     if (o.verbose) fprintf(stderr, "GPUMPI: kernel finished in %.3f s\n", now_s() - t0);
     fflush(stderr);
     cudaEventDestroy(done);
@@ -469,5 +492,5 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     cudaFree(dslots);
     cudaFree(dargs);
     cudaFree(base);
-    return exit_code;
+    return res.exit_code;
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <string>
 #include <vector>
 
 #include "gpumpi.h"
@@ -31,5 +32,20 @@ size_t job_footprint(const gpumpi_opts& o, int n);
 int host_job_init(HostJob& hj, cudaStream_t st);
 int choose_threads(const void* kernel, int n, int requested, size_t smem, int* max_resident);
 void set_last_error(const char* msg);
+
+// Device image of a program's argv (pointer table + strings, relocated to `dev`).
+size_t argv_image_bytes(int argc, char** argv);
+void argv_image(int argc, char** argv, char* dev, std::vector<char>& img);
+
+// What a finished job left in its memory, copied back by job_collect.
+struct JobResult {
+    int status[16];
+    std::vector<int> rets;
+    std::string out, err, errmsg, diag;
+    bool truncated = false;
+    int exit_code = 0;
+};
+int job_collect(HostJob& hj, cudaStream_t st, JobResult& r);
+double now_seconds();
 
 }  // namespace gm

@@ -248,9 +248,11 @@ static __device__ void fold_vec(T* out, const Pub* pub, int nin, u64 in_off, u64
     if (done < n) fold_scalar<T, O>(out + done, pub, nin, in_off, lo + done, hi, tid, T_);
 }
 
+// One out-of-line function per (type, operator): each gets its own register
+// allocation instead of sharing one across the whole dispatch switch.
 template <class T, class O>
-static __device__ void fold_t(void* outv, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
-                              int tid, int T_) {
+static __device__ __noinline__ void fold_t(void* outv, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
+                                           int tid, int T_) {
     T* out = reinterpret_cast<T*>(outv);
     if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
         bool aligned = ((uintptr_t)out & 15) == 0;

@@ -304,10 +304,7 @@ static __device__ __forceinline__ int req_is_done(MPI_Request_impl* r) {
 static __device__ int wait_check(u64 t0, int did, unsigned* ns, const char* what) {
     BlockCtx& b = bctx();
     Job* j = b.job;
-    if (job_aborted(j)) {
-        int code = ld_acquire_int(&j->status[1]);
-        return code ? code : GPUMPI_ERR_ABORTED;
-    }
+    if (job_aborted(j)) return fail_code(j);
     if (gtime() - t0 > j->timeout_ns) {
         job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, what);
         return GPUMPI_ERR_TIMEOUT;

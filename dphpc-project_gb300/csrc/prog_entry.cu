@@ -3,6 +3,8 @@
 // (it calls the program's __gpu_main, which the runtime library alone lacks).
 // Counterpart of __gpu_main_caller and main in gpu_libs/gpu_main/main.cu:103-322.
 #include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "gpumpi.h"
 #include "rt.cuh"
@@ -14,16 +16,23 @@ namespace gm {
 __device__ bool program_block_begin(const Launch& L);
 }
 
+// The name converted programs use for the start of dynamic shared memory
+// (include/gpumpi/global_vars.cuh); it must alias the runtime's block context.
+extern __shared__ __align__(16) char __gpumpi_dsmem[];
+
 extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Launch L) {
     using namespace gm;
     if (!program_block_begin(L)) return;
     BlockCtx& b = bctx();
     if (threadIdx.x == 0) {
         int rc;
-        if ((int)gridDim.x > __gpu_max_threads()) {
+        if (L.slot_base + (int)gridDim.x > __gpu_max_threads()) {
             job_fail(b.job, b.rank, MPI_ERR_INTERN,
-                     "grid exceeds the per-rank global arrays the program was compiled with "
+                     "rank slots exceed the per-rank global arrays the program was compiled with "
                      "(GPU_MPI_MAX_RANKS)");
+            rc = 1;
+        } else if ((const void*)__gpumpi_dsmem != (const void*)&b) {
+            job_fail(b.job, b.rank, MPI_ERR_INTERN, "per-rank globals cannot find the rank slot");
             rc = 1;
         } else {
             rc = __gpu_main(b.job->argc, b.job->argv);
@@ -37,6 +46,17 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Lau
 }
 
 extern "C" int gpumpi_main(int argc, char** argv) {
+    for (int i = 1; i < argc; i++) {
+        if (strcmp(argv[i], "---gpumpi") != 0) continue;
+        for (int k = i + 1; k < argc; k++)
+            if (strcmp(argv[k], "--serve") == 0) {
+                // jobs run as concurrent kernels on their own streams: give them
+                // enough hardware queues (read when the CUDA context is created)
+                setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+                return gpumpi_serve_main((const void*)gpumpi_program_kernel, argc, argv);
+            }
+        break;
+    }
     gpumpi_opts o;
     int pos = gpumpi_parse_args(argc, argv, &o);
     if (pos == -1) {

@@ -232,9 +232,15 @@ struct Heap {
     u32* cls_count;               // [NCLS]
     u32* cls_hint;                // [NCLS * 32]
     u32* next_page;               // bump pointer (1 word)
-    u64* large_free;              // [LARGE_BUCKETS] tagged stack heads
+    u32* large_head;              // free large runs, address order (page + 1, 0 = none)
+    u32* large_lock;              // lock of that list
+    u64* partial;                 // [NCLS] tagged stacks of pages with free chunks
     u32* stats;                   // [8] counters
 };
+
+// Host set-up of a heap's control words (one zeroed block of heap_ctl_bytes()).
+__host__ size_t heap_ctl_bytes();
+__host__ void heap_set_ctl(Heap& h, char* ctl);
 
 // One MPI job (a converted program instance with its own MPI_COMM_WORLD).
 struct Job {
@@ -278,6 +284,7 @@ struct Launch {
     int nslots;
     int* slot_job;                // [nslots], -1 = idle
     int* slot_rank;               // [nslots]
+    int slot_base;                // rank slot of block 0 (launches that run at once use disjoint ranges)
 };
 
 
@@ -399,12 +406,14 @@ struct Call {
     };
 };
 
-// Block-wide context, at offset 0 of dynamic shared memory.
+// Block-wide context, at offset 0 of dynamic shared memory.  `slot` comes
+// first: converted programs index their per-rank globals with the int at the
+// start of dynamic shared memory (include/gpumpi/global_vars.cuh).
 struct BlockCtx {
+    int slot;                     // rank slot, unique among all ranks running at once
+    int rank;                     // rank in the job (MPI_COMM_WORLD rank)
     Job* job;
     RankPriv* priv;
-    int rank;                     // rank in the job (MPI_COMM_WORLD rank)
-    int slot;
     int T;                        // threads in the block
     int leader_mode;              // 1: thread 0 runs user code, others are helpers
     Call call;
@@ -438,6 +447,8 @@ struct BlockCtx {
     int in_call;                  // leader is inside block_call (helpers busy)
 };
 
+static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");
+
 __device__ __forceinline__ BlockCtx& bctx() {
     extern __shared__ __align__(16) char gm_dsmem[];
     return *reinterpret_cast<BlockCtx*>(gm_dsmem);
@@ -467,6 +478,7 @@ __device__ __forceinline__ bool job_aborted(const Job* j) {
 }
 // Record the first error of the job (code, rank, message) and raise the abort flag.
 __device__ void job_fail(Job* j, int rank, int code, const char* msg);
+__device__ int fail_code(Job* j);
 
 // Bounded wait helpers.  Return MPI_SUCCESS, GPUMPI_ERR_TIMEOUT or GPUMPI_ERR_ABORTED.
 __device__ int wait_ge(const u64* addr, u64 target);

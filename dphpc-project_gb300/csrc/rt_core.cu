@@ -34,10 +34,16 @@ __device__ void job_fail(Job* j, int rank, int code, const char* msg) {
     atomicExch(&j->status[0], 1);
 }
 
-static __device__ __forceinline__ int wait_fail(Job* j) {
-    int code = ld_acquire_int(&j->status[1]);
-    return code ? code : GPUMPI_ERR_ABORTED;
+// Code returned by a wait that ended because the job failed: the rank that
+// recorded the job's first error gets that error (e.g. its own timeout); every
+// rank released by another rank's failure gets GPUMPI_ERR_ABORTED.
+__device__ int fail_code(Job* j) {
+    const int code = ld_acquire_int(&j->status[1]);
+    if (code && ld_acquire_int(&j->status[2]) == bctx().rank) return code;
+    return GPUMPI_ERR_ABORTED;
 }
+
+static __device__ __forceinline__ int wait_fail(Job* j) { return fail_code(j); }
 
 __device__ int wait_ge(const u64* addr, u64 target) {
     if (ld_acquire(addr) >= target) return MPI_SUCCESS;
@@ -326,7 +332,7 @@ __device__ bool program_block_begin(const Launch& L) {
             b.job = &L.jobs[jid];
             b.rank = L.slot_rank[slot];
             b.priv = &b.job->priv[b.rank];
-            b.slot = slot;
+            b.slot = L.slot_base + slot;
             b.T = (int)blockDim.x;
             b.leader_mode = 1;
             b.in_call = 0;

@@ -73,3 +73,26 @@ def load_library() -> ctypes.CDLL:
     if not os.path.exists(LIB):
         raise FileNotFoundError(f"{LIB} missing: the CUDA runtime is not built")
     return ctypes.CDLL(LIB, mode=ctypes.RTLD_GLOBAL)
+
+
+class ChurnStats(ctypes.Structure):
+    """gpumpi_churn_stats of include/gpumpi.h."""
+    _fields_ = [("allocs", ctypes.c_uint64), ("frees", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("corrupt", ctypes.c_uint64), ("misaligned", ctypes.c_uint64), ("seconds", ctypes.c_double),
+                ("ops_per_s", ctypes.c_double), ("malloc_cycles_p50", ctypes.c_uint64),
+                ("malloc_cycles_p99", ctypes.c_uint64)]
+
+
+def malloc_churn(lib: ctypes.CDLL, blocks: int, threads: int, iters: int, live: int = 8, seed: int = 1,
+                 heap_bytes: int = 0, cuda_heap: bool = False) -> dict:
+    """Run gpumpi_malloc_churn (every thread loops malloc/fill/verify/free) and return its stats."""
+    f = lib.gpumpi_malloc_churn
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_size_t,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ChurnStats)]
+    f.restype = ctypes.c_int
+    lib.gpumpi_last_error.restype = ctypes.c_char_p
+    st = ChurnStats()
+    rc = f(blocks, threads, iters, live, seed, heap_bytes, int(cuda_heap), None, ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"gpumpi_malloc_churn failed ({rc}): {lib.gpumpi_last_error().decode()}")
+    return {k: getattr(st, k) for k, _ in ChurnStats._fields_}

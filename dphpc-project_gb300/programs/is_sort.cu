@@ -1,0 +1,197 @@
+// Integer bucket sort in the style of the NAS IS kernel, as an MPI program
+// (converter-output form).  Written from the algorithm's description; no NPB
+// source, key generator or verification table is used.
+//
+// Keys: total_keys int32 values spread evenly over the ranks,
+// key = floor(2^max_lg * (u1+u2+u3+u4)/4) with u uniform in [0,1) from a
+// splitmix64 stream seeded by (rank, index).  Buckets: 2^nb_lg by the key's top
+// bits.  Each of `iters` iterations (numbered 1..iters):
+//   1. rank 0 overwrites two keys: key[it] = it, key[it+iters] = max_key - it
+//      (the per-iteration perturbation of IS, is.c:647-650)
+//   2. local bucket histogram, MPI_Allreduce(SUM) of the histograms
+//   3. buckets are assigned to ranks in order, each rank taking buckets until
+//      its cumulative share of the total reaches (r+1)/P
+//   4. MPI_Alltoall of the per-destination key counts
+//   5. local bucket sort into the send buffer, MPI_Alltoallv of the keys
+//   6. counting sort of the received keys over the rank's key range
+// Rank 0 prints one checksum line per iteration (received counts and a hash
+// of each rank's key-rank array, reduced in rank order), then after the last
+// iteration the full verification: every rank's keys nondecreasing and each
+// rank's first key >= the previous rank's last key.
+// Usage: is_sort [log2(total keys)=23] [iters=10] [log2(max key)=19] [log2(buckets)=10]
+#include "global_vars.cuh"
+#include "mpi.h.cuh"
+#include "stdio.h.cuh"
+#include "stdlib.h.cuh"
+#include "string.h.cuh"
+
+__device__ unsigned long long mix64(unsigned long long x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Four uniforms in [0, 2^16) from one 64-bit hash; their sum scaled to the key range.
+__device__ int make_key(int rank, long i, int max_lg) {
+    unsigned long long h = mix64(((unsigned long long)rank << 44) ^ (unsigned long long)i);
+    unsigned long long s = (h & 0xffff) + ((h >> 16) & 0xffff) + ((h >> 32) & 0xffff) + (h >> 48);
+    // (u1+u2+u3+u4)/4 with u = v / 2^16, times 2^max_lg
+    return (int)((s << max_lg) >> 18);
+}
+
+__device__ int __gpu_main(int argc, char** argv) {
+    int rank, size;
+    MPI_Init(&argc, &argv);
+    MPI_Comm_rank(MPI_COMM_WORLD, &rank);
+    MPI_Comm_size(MPI_COMM_WORLD, &size);
+    const int total_lg = argc > 1 ? atoi(argv[1]) : 23;
+    const int iters = argc > 2 ? atoi(argv[2]) : 10;
+    const int max_lg = argc > 3 ? atoi(argv[3]) : 19;
+    const int nb_lg = argc > 4 ? atoi(argv[4]) : 10;
+    const long total = 1L << total_lg;
+    const long nkeys = total / size + (rank < total % size ? 1 : 0);
+    const int max_key = 1 << max_lg;
+    const int nbuckets = 1 << nb_lg;
+    const int shift = max_lg - nb_lg;
+
+    int* keys = (int*)malloc(sizeof(int) * (nkeys > 0 ? nkeys : 1));
+    int* sendk = (int*)malloc(sizeof(int) * (nkeys > 0 ? nkeys : 1));
+    int* hist = (int*)malloc(sizeof(int) * nbuckets);
+    int* ghist = (int*)malloc(sizeof(int) * nbuckets);
+    int* bstart = (int*)malloc(sizeof(int) * nbuckets);
+    int* owner = (int*)malloc(sizeof(int) * nbuckets);
+    int* scount = (int*)malloc(sizeof(int) * size);
+    int* rcount = (int*)malloc(sizeof(int) * size);
+    int* sdispl = (int*)malloc(sizeof(int) * size);
+    int* rdispl = (int*)malloc(sizeof(int) * size);
+    int* recvk = nullptr;
+    int* sorted = nullptr;
+    int* cnt = nullptr;
+    long rcap = 0;
+    int lo_key = 0, hi_key = 0;
+    long nrecv = 0;
+    for (long i = 0; i < nkeys; i++) keys[i] = make_key(rank, i, max_lg);
+
+    MPI_Barrier(MPI_COMM_WORLD);
+    const double t0 = MPI_Wtime();
+    for (int it = 1; it <= iters; it++) {
+        if (rank == 0 && nkeys > it + iters) {
+            keys[it] = it;
+            keys[it + iters] = max_key - it;
+        }
+        for (int b = 0; b < nbuckets; b++) hist[b] = 0;
+        for (long i = 0; i < nkeys; i++) hist[keys[i] >> shift]++;
+        MPI_Allreduce(hist, ghist, nbuckets, MPI_INT, MPI_SUM, MPI_COMM_WORLD);
+        // bucket ownership: rank r takes buckets while its cumulative share < (r+1)/P
+        long acc = 0;
+        int r = 0;
+        for (int b = 0; b < nbuckets; b++) {
+            owner[b] = r;
+            acc += ghist[b];
+            while (r < size - 1 && acc * size >= (long)(r + 1) * total) r++;
+        }
+        for (int q = 0; q < size; q++) scount[q] = 0;
+        for (int b = 0; b < nbuckets; b++) scount[owner[b]] += hist[b];
+        MPI_Alltoall(scount, 1, MPI_INT, rcount, 1, MPI_INT, MPI_COMM_WORLD);
+        // local bucket sort into the send buffer (buckets in order = destinations in order)
+        int off = 0;
+        for (int b = 0; b < nbuckets; b++) {
+            bstart[b] = off;
+            off += hist[b];
+        }
+        for (long i = 0; i < nkeys; i++) sendk[bstart[keys[i] >> shift]++] = keys[i];
+        sdispl[0] = 0;
+        rdispl[0] = 0;
+        for (int q = 1; q < size; q++) {
+            sdispl[q] = sdispl[q - 1] + scount[q - 1];
+            rdispl[q] = rdispl[q - 1] + rcount[q - 1];
+        }
+        nrecv = (long)rdispl[size - 1] + rcount[size - 1];
+        if (nrecv > rcap) {
+            free(recvk);
+            free(sorted);
+            rcap = nrecv + nrecv / 8 + 64;
+            recvk = (int*)malloc(sizeof(int) * rcap);
+            sorted = (int*)malloc(sizeof(int) * rcap);
+        }
+        MPI_Alltoallv(sendk, scount, sdispl, MPI_INT, recvk, rcount, rdispl, MPI_INT, MPI_COMM_WORLD);
+        // key range of this rank's buckets
+        int first_b = -1, last_b = -1;
+        for (int b = 0; b < nbuckets; b++)
+            if (owner[b] == rank) {
+                if (first_b < 0) first_b = b;
+                last_b = b;
+            }
+        lo_key = first_b < 0 ? 0 : first_b << shift;
+        hi_key = first_b < 0 ? 0 : (last_b + 1) << shift;
+        const int range = hi_key - lo_key;
+        if (!cnt) cnt = (int*)malloc(sizeof(int) * (max_key + 1));
+        for (int k = 0; k <= range; k++) cnt[k] = 0;
+        long bad = 0;
+        for (long i = 0; i < nrecv; i++) {
+            const int k = recvk[i] - lo_key;
+            if (k < 0 || k >= range) bad++;
+            else cnt[k + 1]++;
+        }
+        for (int k = 0; k < range; k++) cnt[k + 1] += cnt[k];   // cnt[k] = rank of the first key k
+        unsigned long long h = (unsigned long long)nrecv * 0x100000001B3ull + (unsigned long long)bad;
+        for (int k = 0; k <= range; k += 1 + range / 64) h = mix64(h ^ (unsigned long long)cnt[k]);
+        unsigned long long hsum = 0;
+        long nsum = 0;
+        MPI_Reduce(&h, &hsum, 1, MPI_UNSIGNED_LONG_LONG, MPI_SUM, 0, MPI_COMM_WORLD);
+        MPI_Reduce(&nrecv, &nsum, 1, MPI_LONG, MPI_SUM, 0, MPI_COMM_WORLD);
+        if (rank == 0) printf("is iteration %d keys %ld checksum %016llx\n", it, nsum, hsum);
+    }
+    const double t1 = MPI_Wtime();
+
+    // full verification: place every received key at its rank, check order locally and across ranks
+    long errors = 0;
+    const int range = hi_key - lo_key;
+    for (long i = 0; i < nrecv; i++) {
+        const int k = recvk[i] - lo_key;
+        if (k >= 0 && k < range) sorted[cnt[k]++] = recvk[i];
+        else errors++;
+    }
+    for (long i = 1; i < nrecv; i++)
+        if (sorted[i - 1] > sorted[i]) errors++;
+    int last = nrecv > 0 ? sorted[nrecv - 1] : -1, prev_last = -1;
+    // pass the largest key seen so far along the ranks, so empty ranks do not break the chain
+    if (rank > 0) MPI_Recv(&prev_last, 1, MPI_INT, rank - 1, 5, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+    if (nrecv > 0 && prev_last > sorted[0]) errors++;
+    if (prev_last > last) last = prev_last;
+    if (rank < size - 1) MPI_Send(&last, 1, MPI_INT, rank + 1, 5, MPI_COMM_WORLD);
+    unsigned long long fold = 0;
+    for (long i = 0; i < nrecv; i++) fold = fold * 0x100000001B3ull + (unsigned long long)sorted[i];
+    long errs = 0, keys_total = 0;
+    unsigned long long fsum = 0;
+    double dt = t1 - t0, tmax = 0;
+    MPI_Reduce(&errors, &errs, 1, MPI_LONG, MPI_SUM, 0, MPI_COMM_WORLD);
+    MPI_Reduce(&nrecv, &keys_total, 1, MPI_LONG, MPI_SUM, 0, MPI_COMM_WORLD);
+    MPI_Reduce(&fold, &fsum, 1, MPI_UNSIGNED_LONG_LONG, MPI_SUM, 0, MPI_COMM_WORLD);
+    MPI_Reduce(&dt, &tmax, 1, MPI_DOUBLE, MPI_MAX, 0, MPI_COMM_WORLD);
+    int status = 0;
+    if (rank == 0) {
+        printf("is verify keys %ld errors %ld sorted-checksum %016llx %s\n", keys_total, errs, fsum,
+               errs == 0 && keys_total == total ? "PASSED" : "FAILED");
+        printf("is-time seconds %.6f Mkeys_per_s %.3f\n", tmax, tmax > 0 ? (double)total * iters / tmax / 1e6 : 0.0);
+        status = errs == 0 && keys_total == total ? 0 : 1;
+    }
+    free(keys);
+    free(sendk);
+    free(hist);
+    free(ghist);
+    free(bstart);
+    free(owner);
+    free(scount);
+    free(rcount);
+    free(sdispl);
+    free(rdispl);
+    free(recvk);
+    free(sorted);
+    free(cnt);
+    MPI_Finalize();
+    return status;
+}
+
+__device__ int __gpu_max_threads() { return 1024; }

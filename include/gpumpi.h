@@ -73,6 +73,53 @@ int gpumpi_run_program(const void* program_kernel, int prog_argc, char** prog_ar
 /* Text of the last device job error of this process. */
 const char* gpumpi_last_error(void);
 
+/* ---- serving: many jobs of one program, admitted by HBM footprint ---- */
+
+/* One job: program arguments (argv[0] first), ranks, device heap, arrival. */
+typedef struct gpumpi_job_spec {
+    int argc;
+    char** argv;
+    int nranks;
+    size_t heap_bytes;       /* 0 = 256 MiB */
+    double submit_s;         /* arrival, seconds after serving starts */
+} gpumpi_job_spec;
+
+typedef struct gpumpi_serve_opts {
+    size_t pool_bytes;       /* HBM reserved for the memory of admitted jobs (0 = half of free memory) */
+    int max_slots;           /* rank blocks that may run at once (0 = what the GPU holds, at most 1024) */
+    int threads_per_rank;    /* 0 = 128 */
+    double timeout_s;        /* bound on every device wait (0 = 60 s) */
+    double max_seconds;      /* wall-clock limit of the whole run (0 = none) */
+    int verbose;
+} gpumpi_serve_opts;
+
+typedef struct gpumpi_job_result {
+    int exit_code;           /* 0 when every rank returned 0 and nothing failed */
+    int error;               /* first device error code of the job (0 = none) */
+    size_t footprint;        /* bytes of the HBM pool the job held */
+    int slot_base;           /* first rank slot of the job (-1 = never admitted) */
+    double submit_s, start_s, end_s;   /* seconds after serving started */
+    char* out;               /* the job's stdout text; release with gpumpi_free */
+    char* err;               /* its stderr text and launcher diagnostics; gpumpi_free */
+} gpumpi_job_result;
+
+/* Run every job to completion.  A job is admitted once it has arrived, its
+ * job memory fits in a free range of the pool and a contiguous range of rank
+ * slots is free (running ranks never exceed what the GPU holds at once); each
+ * admitted job is a cooperative launch of program_kernel on its own stream.
+ * No counterpart in the reference, which ran one program per process
+ * (gpu_libs/gpu_main/main.cu:163-321).  Returns 0, GPUMPI_EJOB when a job
+ * failed (see its result), or an error code. */
+int gpumpi_serve(const void* program_kernel, const gpumpi_job_spec* jobs, int njobs,
+                 const gpumpi_serve_opts* opts, gpumpi_job_result* results);
+
+/* Command-line form, used by gpumpi_main when "--serve JOBFILE" follows
+ * "---gpumpi": one job per line, "<ranks> <arrival-ms> [arguments...]". */
+int gpumpi_serve_main(const void* program_kernel, int argc, char** argv);
+
+/* Release memory returned by the runtime (gpumpi_job_result texts). */
+void gpumpi_free(void* p);
+
 /* ---- host-driven collectives (section 2) ---- */
 
 typedef struct gpumpi_comm_s* gpumpi_comm_t;
@@ -165,6 +212,31 @@ int gpumpi_api_status(char* msg, int len);
 int gpumpi_allreduce_noalloc(void* const* sendbufs, void* const* recvbufs, int nranks,
                              uint64_t count, int dtype, int redop, int threads_per_rank,
                              void* stream);
+
+/* ---- allocator churn ---- */
+
+/* Result of gpumpi_malloc_churn. */
+typedef struct gpumpi_churn_stats {
+    uint64_t allocs;              /* malloc calls */
+    uint64_t frees;               /* free calls */
+    uint64_t failed;              /* malloc calls that returned NULL */
+    uint64_t corrupt;             /* objects whose pattern did not survive until free */
+    uint64_t misaligned;          /* pointers not 16-byte aligned */
+    double seconds;               /* kernel time (CUDA events) */
+    double ops_per_s;             /* (allocs + frees) / seconds */
+    uint64_t malloc_cycles_p50;   /* malloc latency percentiles in SM cycles */
+    uint64_t malloc_cycles_p99;   /*   (lower edge of a quarter-octave bucket) */
+} gpumpi_churn_stats;
+
+/* Every thread of a blocks x threads grid runs `iters` rounds of: malloc of
+ * floor(2^U) bytes, U uniform in [4, 12); write a pattern over the object; keep
+ * at most `live` objects (1..16), verifying and freeing the oldest first.
+ * cuda_heap = 0 uses the runtime's slab allocator on a fresh heap of
+ * heap_bytes (0 = 4 GiB); cuda_heap = 1 uses CUDA's device malloc/free, the
+ * allocator behind the reference's __gpu_malloc (gpu_libs/gpu_libc/stdlib.cu:70-91).
+ * Allocates and frees its own device memory; synchronises `stream`. */
+int gpumpi_malloc_churn(int blocks, int threads, int iters, int live, uint64_t seed, size_t heap_bytes,
+                        int cuda_heap, void* stream, gpumpi_churn_stats* out);
 
 /* Number of kernel launches this process issued through the collective API. */
 uint64_t gpumpi_kernel_launches(void);

@@ -33,3 +33,81 @@ def test_gpu_coll_bench_matches_oracle(gpu_built, lg, iters, ranks):
     assert g.returncode == 0, g.stderr[-2000:]
     assert c.returncode == 0, c.stderr[-2000:]
     assert g.lines("coll_bench checksum") == c.lines("coll_bench checksum")
+
+
+P2P_CASES = [
+    ("pairs", "block", 3, 16, 10, 2, "1G"),
+    ("ring", "block", 3, 14, 10, 7, "1G"),
+    ("pairs", "nb", 3, 20, 5, 64, "1G"),
+    ("ring", "nb", 10, 22, 3, 256, "4G"),
+    ("ring", "block", 3, 12, 4, 1024, "1G"),
+    ("pairs", "nb", 24, 26, 2, 8, "2G"),
+]
+
+
+@pytest.mark.parametrize("pattern,mode,lo,hi,iters,ranks,heap", P2P_CASES)
+def test_gpu_p2p_sweep_matches_oracle(gpu_built, pattern, mode, lo, hi, iters, ranks, heap):
+    """Point-to-point sweep: every payload arrives intact (errors 0) and the
+    per-size checksums of the received bytes equal the host MPI run's."""
+    args = [pattern, mode, str(lo), str(hi), str(iters)]
+    g = gpu_built.run_program("p2p_sweep", args, nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=300)
+    c = gpu_built.run_oracle("p2p_sweep", args, nranks=ranks, timeout=300)
+    assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
+    assert c.returncode == 0, c.stderr[-2000:]
+    got = g.lines("p2p ")
+    assert len(got) == hi - lo + 1
+    assert all(" errors 0 " in ln for ln in got)
+    assert got == c.lines("p2p ")
+
+
+@pytest.mark.parametrize("args,ranks", [(["23", "10"], 64), (["14", "3"], 7), (["12", "2"], 1),
+                                        (["20", "4", "19", "10"], 256), (["10", "2"], 64)])
+def test_gpu_is_sort_matches_oracle(gpu_built, args, ranks):
+    """IS-like bucket sort: globally sorted, and every per-iteration checksum and
+    the sorted-key checksum equal the host MPI run's."""
+    g = gpu_built.run_program("is_sort", args, nranks=ranks, extra=GPU_OPTS + ["-p", "2G"], timeout=300)
+    c = gpu_built.run_oracle("is_sort", args, nranks=ranks, timeout=300)
+    assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
+    assert c.returncode == 0, c.stderr[-2000:]
+    assert g.lines("is verify")[0].endswith("PASSED")
+    assert g.lines("is ") == c.lines("is ")
+
+
+def _pic_values(res):
+    out = []
+    for ln in res.lines("pic cycle"):
+        w = ln.split()
+        out.append((int(w[2]), int(w[4]), [float(w[i]) for i in (6, 8, 10, 12)]))
+    return out
+
+
+@pytest.mark.parametrize("args,ranks,heap", [(["10", "64", "32", "20", "5"], 16, "1G"),
+                                             (["20", "32", "16", "20", "5"], 4, "1G"),
+                                             (["6", "16", "8", "10", "3"], 1, "1G"),
+                                             (["50", "256", "128", "125", "10"], 64, "4G")])
+def test_gpu_pic_matches_oracle(gpu_built, args, ranks, heap):
+    """PIC mini-app: energies within 1e-10 relative of the host MPI run (the
+    stated tolerance; the arithmetic is + - * / only, so they agree bit for
+    bit) and the same particle count and position checksum."""
+    g = gpu_built.run_program("pic", args, nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=600)
+    c = gpu_built.run_oracle("pic", args, nranks=ranks, timeout=600)
+    assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
+    assert c.returncode == 0, c.stderr[-2000:]
+    gv, cv = _pic_values(g), _pic_values(c)
+    assert len(gv) == len(cv) > 0
+    for (gc, gn, ge), (cc, cn, ce) in zip(gv, cv):
+        assert gc == cc and gn == cn
+        for a, b in zip(ge, ce):
+            assert abs(a - b) <= 1e-10 * abs(b)
+    assert g.lines("pic positions") == c.lines("pic positions")
+    assert g.lines("pic cycle") == c.lines("pic cycle")
+
+
+@pytest.mark.parametrize("ranks,heap", [(4, "1G"), (64, "4G"), (1, "64M")])
+def test_gpu_allocator_known_answers(gpu_built, ranks, heap):
+    """Device malloc: sizes 1 B .. 4 MiB aligned and disjoint, reuse after free,
+    calloc zeros, realloc keeps the prefix.  With one rank and a 64 MiB heap
+    the growing large blocks fit only if freed runs are merged."""
+    g = gpu_built.run_program("kat_malloc", [], nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=300)
+    assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
+    assert sorted(g.lines("kat_malloc")) == sorted(f"kat_malloc rank {r} ok" for r in range(ranks))
