@@ -64,6 +64,14 @@ __device__ __noinline__ int dispatch_all(int tid) {
         case OP_MEMCPY: blk_copy((void*)c.a[0], (const void*)c.a[1], c.a[2], tid, T); break;
         case OP_MEMSET: blk_memset((void*)c.a[0], (int)c.a[1], c.a[2], tid, T); break;
         case OP_FINALIZE: rc = finalize_block(tid, T); break;
+        case OP_PARFOR: {
+            // every thread of the rank block runs a share of the iterations
+            void (*body)(long, void*) = (void (*)(long, void*))c.a[0];
+            void* arg = (void*)c.a[1];
+            const long n = (long)c.a[2];
+            for (long i = tid; i < n; i += T) body(i, arg);
+            break;
+        }
         default: rc = MPI_ERR_INTERN; break;
     }
     bsync();

@@ -173,6 +173,29 @@ static __device__ bool can_fan_out(u64 n) {
 
 __device__ void* __gpu_malloc(size_t size) { return heap_alloc(&bctx().job->heap, size); }
 
+// Parallel loop over the rank's whole thread block.  The leader hands the loop
+// to the block like an MPI call; each thread runs iterations tid, tid+T, ...;
+// the call returns after a block barrier, so every iteration's writes are
+// visible to the leader.  `arg` is passed to every thread, so it must point to
+// memory all threads can read (heap, globals); pointers into the leader's
+// local memory, nested calls and calls from inside an MPI call run the loop
+// on the leader alone, in order.
+__device__ void __gpu_parallel_for(long n, __gpu_loop_body body, void* arg) {
+    BlockCtx& b = bctx();
+    if (n <= 0) return;
+    const bool fan = n > 1 && b.leader_mode && threadIdx.x == 0 && !b.in_call && (arg == nullptr || is_global(arg));
+    if (!fan) {
+        for (long i = 0; i < n; i++) body(i, arg);
+        return;
+    }
+    Call call;
+    call.op = OP_PARFOR;
+    call.a[0] = (u64)body;
+    call.a[1] = (u64)arg;
+    call.a[2] = (u64)n;
+    block_call(call);
+}
+
 __device__ void* __gpu_memset(void* s, int c, size_t n) {
     if (can_fan_out(n) && is_global(s)) {
         Call call;

@@ -61,6 +61,7 @@ enum CallOp : int {
     OP_MEMCPY,
     OP_MEMSET,
     OP_FINALIZE,
+    OP_PARFOR,
     OP_NUM
 };
 

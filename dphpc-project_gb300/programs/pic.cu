@@ -13,20 +13,33 @@
 //     MPI_Isend / MPI_Irecv of counts and then of malloc'd variable-size
 //     buffers;
 //   * kinetic and field energies are summed with MPI_Allreduce.
+//
+// The particle and grid loops run through gpumpi_parallel_for (omp.h.cuh):
+// on the GPU over the rank's whole thread block, in a host build in order.
+// Both give the same bits because nothing depends on the order in which
+// iterations run: particles are cut into `nchunk` fixed chunks of consecutive
+// particles whatever the thread count, energies are summed per chunk and the
+// chunks' sums added in chunk order, particles that leave are listed chunk by
+// chunk (so every buffer keeps the order of a serial loop), and currents are
+// deposited in 64-bit fixed point (2^-40 units, truncated), whose sums are
+// exact in any order (gpumpi_atomic_add_i64: an atomic add on the GPU, a plain
+// add on the host).
+//
 // Initial state: PPC particles per cell and species at seeded uniform
 // positions, thermal velocities by the Irwin-Hall sum of 12 uniforms (only
-// additions, so the host and GPU builds draw identical values), electrons in
-// two counter-streaming beams (+-0.1) so that particles migrate.  All
-// arithmetic is + - * / on doubles in a fixed order: a GPU run (-fmad=false)
-// and a host MPI run give the same bits.
+// additions), electrons in two counter-streaming beams (+-0.1) so that
+// particles migrate.  All arithmetic is + - * / on doubles in a fixed order:
+// a GPU run (-fmad=false) and a host MPI run give the same bits.
 // Rank 0 prints the energies every `report` cycles and a checksum of all
 // particle positions at the end.
-// Usage: pic [cycles=50] [GX=256] [GY=128] [PPC=125] [report=10]   (P ranks: PX*PY = P, PX >= PY)
+// Usage: pic [cycles=50] [GX=256] [GY=128] [PPC=125] [report=10] [nchunk=1024]
+//        (P ranks as PX x PY with PX >= PY, the most square split)
 #include "global_vars.cuh"
 #include "mpi.h.cuh"
 #include "stdio.h.cuh"
 #include "stdlib.h.cuh"
 #include "string.h.cuh"
+#include "omp.h.cuh"
 
 #define NSPEC 2
 
@@ -50,22 +63,44 @@ struct Species {
     double* v;
     long n;
     long cap;
+    double* ax;     // spare arrays: the compaction target, swapped with x..v
+    double* ay;
+    double* au;
+    double* av;
+    long alt_cap;
     double qm;      // charge / mass
     double qw;      // charge of one macro-particle
     double mw;      // mass of one macro-particle
 };
 
-// Local grid: (nx+2) x (ny+2) with one ghost layer, index (i+1) + (j+1)*(nx+2).
-struct Grid {
-    int nx, ny, x0, y0, GX, GY;
+// Everything the parallel loops read or write, in the heap.
+struct Pic {
+    // grid: (nx+2) x (ny+2) with one ghost layer, index (i+1) + (j+1)*(nx+2)
+    int nx, ny, x0, y0, GX, GY, PX, PY, bx, by, cells, nchunk;
+    double dt;
     double* ex;
     double* ey;
     double* bz;
     double* jx;
     double* jy;
+    long long* ajx;          // [cells] fixed-point current accumulators
+    long long* ajy;
+    double* part;            // [nchunk][4] per-chunk partial sums
+    Species sp[NSPEC];
+    int s;                   // species of the running loop
+    // migration
+    signed char* dest;       // [n] neighbour index 0..7 of each particle, -1 = stays
+    int* ccount;             // [nchunk][9] per chunk: leavers per neighbour, stayers
+    long* coff;              // [nchunk][9] write offsets
+    double* sbuf[8];         // outgoing particles per neighbour (4 doubles each)
 };
 
-__device__ int gid(const Grid* g, int i, int j) { return (i + 1) + (j + 1) * (g->nx + 2); }
+__device__ int gid(const Pic* g, int i, int j) { return (i + 1) + (j + 1) * (g->nx + 2); }
+
+__device__ void chunk_range(long n, int nchunk, int c, long* k0, long* k1) {
+    *k0 = n * c / nchunk;
+    *k1 = n * (c + 1) / nchunk;
+}
 
 __device__ int reserve(Species* s, long need) {
     if (need <= s->cap) return 0;
@@ -101,16 +136,14 @@ __device__ int block_rank(int bx, int by, int PX, int PY) {
 }
 
 // Copy ghost layers of field f: x direction (columns), then y (rows incl. ghost columns).
-__device__ void halo_fill(Grid* g, double* f, double* sb, double* rb, int left, int right, int down, int up) {
+__device__ void halo_fill(Pic* g, double* f, double* sb, double* rb, int left, int right, int down, int up) {
     const int nx = g->nx, ny = g->ny, W = nx + 2;
-    // x: send my last owned column to the right, receive my left ghost from the left
     for (int j = 0; j < ny; j++) sb[j] = f[gid(g, nx - 1, j)];
     MPI_Sendrecv(sb, ny, MPI_DOUBLE, right, 11, rb, ny, MPI_DOUBLE, left, 11, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
     for (int j = 0; j < ny; j++) f[gid(g, -1, j)] = rb[j];
     for (int j = 0; j < ny; j++) sb[j] = f[gid(g, 0, j)];
     MPI_Sendrecv(sb, ny, MPI_DOUBLE, left, 12, rb, ny, MPI_DOUBLE, right, 12, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
     for (int j = 0; j < ny; j++) f[gid(g, nx, j)] = rb[j];
-    // y: whole rows including the ghost columns
     for (int i = -1; i <= nx; i++) sb[i + 1] = f[gid(g, i, ny - 1)];
     MPI_Sendrecv(sb, W, MPI_DOUBLE, up, 13, rb, W, MPI_DOUBLE, down, 13, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
     for (int i = -1; i <= nx; i++) f[gid(g, i, -1)] = rb[i + 1];
@@ -120,7 +153,7 @@ __device__ void halo_fill(Grid* g, double* f, double* sb, double* rb, int left, 
 }
 
 // Add ghost contributions of f to the owners: y rows first (incl. ghost columns), then x columns.
-__device__ void halo_add(Grid* g, double* f, double* sb, double* rb, int left, int right, int down, int up) {
+__device__ void halo_add(Pic* g, double* f, double* sb, double* rb, int left, int right, int down, int up) {
     const int nx = g->nx, ny = g->ny, W = nx + 2;
     for (int i = -1; i <= nx; i++) sb[i + 1] = f[gid(g, i, ny)];
     MPI_Sendrecv(sb, W, MPI_DOUBLE, up, 21, rb, W, MPI_DOUBLE, down, 21, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
@@ -137,7 +170,7 @@ __device__ void halo_add(Grid* g, double* f, double* sb, double* rb, int left, i
 }
 
 // Cloud-in-cell weights of a position relative to the local block.
-__device__ void cic(const Grid* g, double px, double py, int* i, int* j, double* fx, double* fy) {
+__device__ void cic(const Pic* g, double px, double py, int* i, int* j, double* fx, double* fy) {
     const double lx = px - (double)g->x0, ly = py - (double)g->y0;
     int ii = (int)lx, jj = (int)ly;
     if (lx < 0.0) ii = -1;
@@ -150,17 +183,176 @@ __device__ void cic(const Grid* g, double px, double py, int* i, int* j, double*
     *fy = ly - (double)jj;
 }
 
-__device__ double interp(const Grid* g, const double* f, int i, int j, double fx, double fy) {
+__device__ double interp(const Pic* g, const double* f, int i, int j, double fx, double fy) {
     const double a = f[gid(g, i, j)] * (1.0 - fx) + f[gid(g, i + 1, j)] * fx;
     const double b = f[gid(g, i, j + 1)] * (1.0 - fx) + f[gid(g, i + 1, j + 1)] * fx;
     return a * (1.0 - fy) + b * fy;
 }
 
-__device__ void deposit(const Grid* g, double* f, int i, int j, double fx, double fy, double val) {
-    f[gid(g, i, j)] += val * (1.0 - fx) * (1.0 - fy);
-    f[gid(g, i + 1, j)] += val * fx * (1.0 - fy);
-    f[gid(g, i, j + 1)] += val * (1.0 - fx) * fy;
-    f[gid(g, i + 1, j + 1)] += val * fx * fy;
+// ---- loop bodies (one call per chunk, cell or row) ----
+
+__device__ void push_chunk(long c, void* arg) {
+    Pic* g = (Pic*)arg;
+    Species* S = &g->sp[g->s];
+    const double dt = g->dt;
+    const double h = 0.5 * S->qm * dt;
+    long k0, k1;
+    chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
+    for (long k = k0; k < k1; k++) {
+        int i, j;
+        double fx, fy;
+        cic(g, S->x[k], S->y[k], &i, &j, &fx, &fy);
+        const double ex = interp(g, g->ex, i, j, fx, fy);
+        const double ey = interp(g, g->ey, i, j, fx, fy);
+        const double bz = interp(g, g->bz, i, j, fx, fy);
+        // Boris: half kick, rotation about z, half kick
+        double um = S->u[k] + h * ex, vm = S->v[k] + h * ey;
+        const double t = h * bz;
+        const double sfac = 2.0 * t / (1.0 + t * t);
+        const double up_ = um + vm * t, vp_ = vm - um * t;
+        um = um + vp_ * sfac;
+        vm = vm - up_ * sfac;
+        S->u[k] = um + h * ex;
+        S->v[k] = vm + h * ey;
+        double nxp = S->x[k] + S->u[k] * dt, nyp = S->y[k] + S->v[k] * dt;
+        if (nxp < 0.0) nxp += (double)g->GX;
+        if (nxp >= (double)g->GX) nxp -= (double)g->GX;
+        if (nyp < 0.0) nyp += (double)g->GY;
+        if (nyp >= (double)g->GY) nyp -= (double)g->GY;
+        S->x[k] = nxp;
+        S->y[k] = nyp;
+    }
+}
+
+// Neighbour index (0..7) of every particle that left the block, -1 for the rest.
+__device__ void classify_chunk(long c, void* arg) {
+    Pic* g = (Pic*)arg;
+    Species* S = &g->sp[g->s];
+    int* cnt = g->ccount + c * 9;
+    for (int q = 0; q < 9; q++) cnt[q] = 0;
+    long k0, k1;
+    chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
+    for (long k = k0; k < k1; k++) {
+        const int cx = (int)S->x[k] / g->nx, cy = (int)S->y[k] / g->ny;
+        int dx = cx - g->bx, dy = cy - g->by;
+        if (dx > 1) dx -= g->PX;
+        if (dx < -1) dx += g->PX;
+        if (dy > 1) dy -= g->PY;
+        if (dy < -1) dy += g->PY;
+        int q = -1;
+        if (dx != 0 || dy != 0) {
+            q = (dy + 1) * 3 + (dx + 1);
+            if (q > 4) q--;
+        }
+        g->dest[k] = (signed char)q;
+        cnt[q < 0 ? 8 : q]++;
+    }
+}
+
+// Leavers go to their neighbour's buffer, stayers to the compacted arrays,
+// each at the offsets of its chunk (so the order is the particle order).
+__device__ void scatter_chunk(long c, void* arg) {
+    Pic* g = (Pic*)arg;
+    Species* S = &g->sp[g->s];
+    long off[9];
+    for (int q = 0; q < 9; q++) off[q] = g->coff[c * 9 + q];
+    long k0, k1;
+    chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
+    for (long k = k0; k < k1; k++) {
+        const int q = g->dest[k];
+        if (q < 0) {
+            const long w = off[8]++;
+            S->ax[w] = S->x[k];
+            S->ay[w] = S->y[k];
+            S->au[w] = S->u[k];
+            S->av[w] = S->v[k];
+        } else {
+            double* d = g->sbuf[q] + 4 * off[q]++;
+            d[0] = S->x[k];
+            d[1] = S->y[k];
+            d[2] = S->u[k];
+            d[3] = S->v[k];
+        }
+    }
+}
+
+#define FIX_ONE 1099511627776.0   // 2^40
+
+__device__ void deposit_fixed(const Pic* g, long long* f, int i, int j, double fx, double fy, double val) {
+    gpumpi_atomic_add_i64(&f[gid(g, i, j)], (long long)(val * (1.0 - fx) * (1.0 - fy) * FIX_ONE));
+    gpumpi_atomic_add_i64(&f[gid(g, i + 1, j)], (long long)(val * fx * (1.0 - fy) * FIX_ONE));
+    gpumpi_atomic_add_i64(&f[gid(g, i, j + 1)], (long long)(val * (1.0 - fx) * fy * FIX_ONE));
+    gpumpi_atomic_add_i64(&f[gid(g, i + 1, j + 1)], (long long)(val * fx * fy * FIX_ONE));
+}
+
+__device__ void clear_current_cell(long k, void* arg) {
+    Pic* g = (Pic*)arg;
+    g->ajx[k] = 0;
+    g->ajy[k] = 0;
+}
+
+// Deposit of one chunk of both species into the fixed-point accumulators.
+__device__ void deposit_chunk(long c, void* arg) {
+    Pic* g = (Pic*)arg;
+    for (int s = 0; s < NSPEC; s++) {
+        const Species* S = &g->sp[s];
+        long k0, k1;
+        chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
+        for (long k = k0; k < k1; k++) {
+            int i, j;
+            double fx, fy;
+            cic(g, S->x[k], S->y[k], &i, &j, &fx, &fy);
+            deposit_fixed(g, g->ajx, i, j, fx, fy, S->qw * S->u[k]);
+            deposit_fixed(g, g->ajy, i, j, fx, fy, S->qw * S->v[k]);
+        }
+    }
+}
+
+__device__ void current_from_fixed_cell(long k, void* arg) {
+    Pic* g = (Pic*)arg;
+    g->jx[k] = (double)g->ajx[k] * (1.0 / FIX_ONE);
+    g->jy[k] = (double)g->ajy[k] * (1.0 / FIX_ONE);
+}
+
+__device__ void bz_half_row(long j, void* arg) {
+    Pic* g = (Pic*)arg;
+    for (int i = 0; i < g->nx; i++) {
+        const double curl = (g->ey[gid(g, i + 1, (int)j)] - g->ey[gid(g, i, (int)j)]) -
+                            (g->ex[gid(g, i, (int)j + 1)] - g->ex[gid(g, i, (int)j)]);
+        g->bz[gid(g, i, (int)j)] -= 0.5 * g->dt * curl;
+    }
+}
+
+__device__ void e_full_row(long j, void* arg) {
+    Pic* g = (Pic*)arg;
+    for (int i = 0; i < g->nx; i++) {
+        const int c = gid(g, i, (int)j);
+        g->ex[c] += g->dt * ((g->bz[c] - g->bz[gid(g, i, (int)j - 1)]) - g->jx[c]);
+        g->ey[c] += g->dt * (-(g->bz[c] - g->bz[gid(g, i - 1, (int)j)]) - g->jy[c]);
+    }
+}
+
+// Per-chunk kinetic sums (both species) and per-row field sums.
+__device__ void energy_chunk(long c, void* arg) {
+    Pic* g = (Pic*)arg;
+    double* e = g->part + c * 4;
+    for (int s = 0; s < NSPEC; s++) {
+        const Species* S = &g->sp[s];
+        long k0, k1;
+        chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
+        double ke = 0.0;
+        for (long k = k0; k < k1; k++) ke += S->u[k] * S->u[k] + S->v[k] * S->v[k];
+        e[s] = ke;
+    }
+    e[2] = 0.0;
+    e[3] = 0.0;
+    if (c < g->ny) {
+        for (int i = 0; i < g->nx; i++) {
+            const int q = gid(g, i, (int)c);
+            e[2] += g->ex[q] * g->ex[q] + g->ey[q] * g->ey[q];
+            e[3] += g->bz[q] * g->bz[q];
+        }
+    }
 }
 
 __device__ int __gpu_main(int argc, char** argv) {
@@ -173,6 +365,7 @@ __device__ int __gpu_main(int argc, char** argv) {
     const int GY = argc > 3 ? atoi(argv[3]) : 128;
     const int PPC = argc > 4 ? atoi(argv[4]) : 125;
     const int report = argc > 5 ? atoi(argv[5]) : 10;
+    int nchunk = argc > 6 ? atoi(argv[6]) : 1024;
     // process grid: the most square PX x PY with PX >= PY
     int PY = 1;
     for (int d = 1; d * d <= size; d++)
@@ -183,24 +376,36 @@ __device__ int __gpu_main(int argc, char** argv) {
         MPI_Finalize();
         return 1;
     }
-    const int bx = rank % PX, by = rank / PX;
-    Grid g;
-    g.nx = GX / PX;
-    g.ny = GY / PY;
-    g.x0 = bx * g.nx;
-    g.y0 = by * g.ny;
-    g.GX = GX;
-    g.GY = GY;
-    const int cells = (g.nx + 2) * (g.ny + 2);
-    double* fields = (double*)calloc((size_t)cells * 5, sizeof(double));
-    g.ex = fields;
-    g.ey = fields + cells;
-    g.bz = fields + 2 * cells;
-    g.jx = fields + 3 * cells;
-    g.jy = fields + 4 * cells;
-    const int hb = (g.nx > g.ny ? g.nx : g.ny) + 2;
+    Pic* g = (Pic*)calloc(1, sizeof(Pic));
+    g->PX = PX;
+    g->PY = PY;
+    g->bx = rank % PX;
+    g->by = rank / PX;
+    g->nx = GX / PX;
+    g->ny = GY / PY;
+    g->x0 = g->bx * g->nx;
+    g->y0 = g->by * g->ny;
+    g->GX = GX;
+    g->GY = GY;
+    g->dt = 0.5;
+    if (nchunk < g->ny) nchunk = g->ny;   // energy rows ride on the chunk loop
+    g->nchunk = nchunk;
+    g->cells = (g->nx + 2) * (g->ny + 2);
+    double* fields = (double*)calloc((size_t)g->cells * 5, sizeof(double));
+    g->ex = fields;
+    g->ey = fields + g->cells;
+    g->bz = fields + 2 * g->cells;
+    g->jx = fields + 3 * g->cells;
+    g->jy = fields + 4 * g->cells;
+    g->ajx = (long long*)malloc(sizeof(long long) * 2 * (size_t)g->cells);
+    g->ajy = g->ajx + g->cells;
+    g->part = (double*)malloc(sizeof(double) * 4 * nchunk);
+    g->ccount = (int*)malloc(sizeof(int) * 9 * nchunk);
+    g->coff = (long*)malloc(sizeof(long) * 9 * nchunk);
+    const int hb = (g->nx > g->ny ? g->nx : g->ny) + 2;
     double* sb = (double*)malloc(sizeof(double) * hb);
     double* rb = (double*)malloc(sizeof(double) * hb);
+    const int bx = g->bx, by = g->by;
     const int left = block_rank(bx - 1, by, PX, PY), right = block_rank(bx + 1, by, PX, PY);
     const int down = block_rank(bx, by - 1, PX, PY), up = block_rank(bx, by + 1, PX, PY);
     int nb[8];
@@ -210,133 +415,97 @@ __device__ int __gpu_main(int argc, char** argv) {
             for (int dx = -1; dx <= 1; dx++)
                 if (dx || dy) nb[k++] = block_rank(bx + dx, by + dy, PX, PY);
     }
-    const double dt = 0.5;
     const double uth[NSPEC] = {0.045, 0.009};
     const double qm[NSPEC] = {-1.0, 1.0 / 25.0};
     // plasma frequency 0.1 for electrons: density 1 per cell, w_p^2 = q^2 n / m
     const double qe = 0.1 / (double)PPC;
-    Species sp[NSPEC];
+    int status = 0;
+    long dest_cap = 0;
     for (int s = 0; s < NSPEC; s++) {
-        sp[s].x = sp[s].y = sp[s].u = sp[s].v = nullptr;
-        sp[s].n = 0;
-        sp[s].cap = 0;
-        sp[s].qm = qm[s];
-        sp[s].qw = s == 0 ? -qe : qe;
-        sp[s].mw = sp[s].qw / sp[s].qm;
-        reserve(&sp[s], (long)g.nx * g.ny * PPC + 64);
+        Species* S = &g->sp[s];
+        S->qm = qm[s];
+        S->qw = s == 0 ? -qe : qe;
+        S->mw = S->qw / S->qm;
+        if (reserve(S, (long)g->nx * g->ny * PPC + 64)) status = 1;
         unsigned long long seed = mix64(((unsigned long long)rank << 8) + (unsigned long long)s + 1);
-        for (int j = 0; j < g.ny; j++)
-            for (int i = 0; i < g.nx; i++)
+        for (int j = 0; j < g->ny && !status; j++)
+            for (int i = 0; i < g->nx; i++)
                 for (int p = 0; p < PPC; p++) {
-                    const long k = sp[s].n++;
-                    sp[s].x[k] = (double)(g.x0 + i) + unif(&seed);
-                    sp[s].y[k] = (double)(g.y0 + j) + unif(&seed);
+                    const long k = S->n++;
+                    S->x[k] = (double)(g->x0 + i) + unif(&seed);
+                    S->y[k] = (double)(g->y0 + j) + unif(&seed);
                     double a = 0.0, b = 0.0;
                     for (int q = 0; q < 12; q++) a += unif(&seed);
                     for (int q = 0; q < 12; q++) b += unif(&seed);
-                    sp[s].u[k] = (a - 6.0) * uth[s] + (s == 0 ? ((p & 1) ? 0.1 : -0.1) : 0.0);
-                    sp[s].v[k] = (b - 6.0) * uth[s];
+                    S->u[k] = (a - 6.0) * uth[s] + (s == 0 ? ((p & 1) ? 0.1 : -0.1) : 0.0);
+                    S->v[k] = (b - 6.0) * uth[s];
                 }
     }
-    // migration scratch: counts and per-neighbour index lists
-    long* out_idx = nullptr;
-    long out_cap = 0;
     MPI_Barrier(MPI_COMM_WORLD);
     const double t0 = MPI_Wtime();
-    int status = 0;
-    for (int cyc = 1; cyc <= cycles; cyc++) {
+    for (int cyc = 1; cyc <= cycles && !status; cyc++) {
         // 1. push and move
-        halo_fill(&g, g.ex, sb, rb, left, right, down, up);
-        halo_fill(&g, g.ey, sb, rb, left, right, down, up);
-        halo_fill(&g, g.bz, sb, rb, left, right, down, up);
+        halo_fill(g, g->ex, sb, rb, left, right, down, up);
+        halo_fill(g, g->ey, sb, rb, left, right, down, up);
+        halo_fill(g, g->bz, sb, rb, left, right, down, up);
         for (int s = 0; s < NSPEC; s++) {
-            Species* S = &sp[s];
-            const double h = 0.5 * S->qm * dt;
-            for (long k = 0; k < S->n; k++) {
-                int i, j;
-                double fx, fy;
-                cic(&g, S->x[k], S->y[k], &i, &j, &fx, &fy);
-                const double ex = interp(&g, g.ex, i, j, fx, fy);
-                const double ey = interp(&g, g.ey, i, j, fx, fy);
-                const double bz = interp(&g, g.bz, i, j, fx, fy);
-                // Boris: half kick, rotation about z, half kick
-                double um = S->u[k] + h * ex, vm = S->v[k] + h * ey;
-                const double t = h * bz;
-                const double sfac = 2.0 * t / (1.0 + t * t);
-                const double up_ = um + vm * t, vp_ = vm - um * t;
-                um = um + vp_ * sfac;
-                vm = vm - up_ * sfac;
-                S->u[k] = um + h * ex;
-                S->v[k] = vm + h * ey;
-                double nxp = S->x[k] + S->u[k] * dt, nyp = S->y[k] + S->v[k] * dt;
-                if (nxp < 0.0) nxp += (double)GX;
-                if (nxp >= (double)GX) nxp -= (double)GX;
-                if (nyp < 0.0) nyp += (double)GY;
-                if (nyp >= (double)GY) nyp -= (double)GY;
-                S->x[k] = nxp;
-                S->y[k] = nyp;
-            }
+            g->s = s;
+            gpumpi_parallel_for(nchunk, push_chunk, g);
         }
         // 2. migrate particles that left the block, species by species
-        for (int s = 0; s < NSPEC; s++) {
-            Species* S = &sp[s];
-            if (S->n > out_cap) {
-                free(out_idx);
-                out_cap = S->cap;
-                out_idx = (long*)malloc(sizeof(long) * out_cap);
-            }
-            int scnt[8], rcnt[8];
-            for (int q = 0; q < 8; q++) scnt[q] = 0;
-            long nout = 0;
-            // classify: neighbour index 0..7 or -1 (stays)
-            for (long k = 0; k < S->n; k++) {
-                int cx = (int)S->x[k] / g.nx, cy = (int)S->y[k] / g.ny;
-                int dx = cx - bx, dy = cy - by;
-                if (dx > 1) dx -= PX;
-                if (dx < -1) dx += PX;
-                if (dy > 1) dy -= PY;
-                if (dy < -1) dy += PY;
-                if (dx == 0 && dy == 0) continue;
-                int q = (dy + 1) * 3 + (dx + 1);
-                if (q > 4) q--;
-                out_idx[nout++] = k * 8 + q;
-                scnt[q]++;
-            }
-            // buffers per neighbour: 4 doubles per particle
-            double* sbuf[8];
-            double* rbuf[8];
-            int fill[8];
-            for (int q = 0; q < 8; q++) {
-                sbuf[q] = (double*)malloc(sizeof(double) * 4 * (scnt[q] > 0 ? scnt[q] : 1));
-                fill[q] = 0;
-            }
-            for (long m = 0; m < nout; m++) {
-                const long k = out_idx[m] / 8;
-                const int q = (int)(out_idx[m] % 8);
-                double* d = sbuf[q] + 4 * fill[q]++;
-                d[0] = S->x[k];
-                d[1] = S->y[k];
-                d[2] = S->u[k];
-                d[3] = S->v[k];
-            }
-            // remove departed particles, keeping the order of the rest
-            {
-                long w = 0, m = 0;
-                for (long k = 0; k < S->n; k++) {
-                    if (m < nout && out_idx[m] / 8 == k) {
-                        m++;
-                        continue;
-                    }
-                    S->x[w] = S->x[k];
-                    S->y[w] = S->y[k];
-                    S->u[w] = S->u[k];
-                    S->v[w] = S->v[k];
-                    w++;
+        for (int s = 0; s < NSPEC && !status; s++) {
+            Species* S = &g->sp[s];
+            g->s = s;
+            if (S->n > dest_cap) {
+                free(g->dest);
+                dest_cap = S->cap;
+                g->dest = (signed char*)malloc(dest_cap);
+                if (!g->dest) {
+                    status = 1;
+                    break;
                 }
-                S->n = w;
             }
+            if (S->n > S->alt_cap) {   // the stayers (at most n) are written to the spare arrays
+                free(S->ax);
+                free(S->ay);
+                free(S->au);
+                free(S->av);
+                S->alt_cap = S->cap;
+                S->ax = (double*)malloc(sizeof(double) * S->alt_cap);
+                S->ay = (double*)malloc(sizeof(double) * S->alt_cap);
+                S->au = (double*)malloc(sizeof(double) * S->alt_cap);
+                S->av = (double*)malloc(sizeof(double) * S->alt_cap);
+                if (!S->ax || !S->ay || !S->au || !S->av) {
+                    status = 1;
+                    break;
+                }
+            }
+            gpumpi_parallel_for(nchunk, classify_chunk, g);
+            int scnt[8], rcnt[8];
+            long stay = 0;
+            for (int q = 0; q < 8; q++) scnt[q] = 0;
+            for (int c = 0; c < nchunk; c++)
+                for (int q = 0; q < 9; q++) {
+                    const int v = g->ccount[c * 9 + q];
+                    g->coff[c * 9 + q] = q == 8 ? stay : (long)scnt[q];
+                    if (q == 8) stay += v;
+                    else scnt[q] += v;
+                }
+            for (int q = 0; q < 8; q++) g->sbuf[q] = (double*)malloc(sizeof(double) * 4 * (scnt[q] > 0 ? scnt[q] : 1));
+            gpumpi_parallel_for(nchunk, scatter_chunk, g);
+            // the compacted arrays become the species' arrays (with their capacity)
+            double* t;
+            t = S->x; S->x = S->ax; S->ax = t;
+            t = S->y; S->y = S->ay; S->ay = t;
+            t = S->u; S->u = S->au; S->au = t;
+            t = S->v; S->v = S->av; S->av = t;
+            const long tc = S->cap;
+            S->cap = S->alt_cap;
+            S->alt_cap = tc;
+            S->n = stay;
             // counts, then data; the message from neighbour q arrives with tag 100 + (7 - q)
             MPI_Request rq[16];
+            double* rbuf[8];
             for (int q = 0; q < 8; q++) {
                 MPI_Irecv(&rcnt[q], 1, MPI_INT, nb[q], 100 + (7 - q), MPI_COMM_WORLD, &rq[q]);
                 MPI_Isend(&scnt[q], 1, MPI_INT, nb[q], 100 + q, MPI_COMM_WORLD, &rq[8 + q]);
@@ -347,7 +516,7 @@ __device__ int __gpu_main(int argc, char** argv) {
                 rbuf[q] = (double*)malloc(sizeof(double) * 4 * (rcnt[q] > 0 ? rcnt[q] : 1));
                 nin += rcnt[q];
                 MPI_Irecv(rbuf[q], 4 * rcnt[q], MPI_DOUBLE, nb[q], 200 + (7 - q), MPI_COMM_WORLD, &rq[q]);
-                MPI_Isend(sbuf[q], 4 * scnt[q], MPI_DOUBLE, nb[q], 200 + q, MPI_COMM_WORLD, &rq[8 + q]);
+                MPI_Isend(g->sbuf[q], 4 * scnt[q], MPI_DOUBLE, nb[q], 200 + q, MPI_COMM_WORLD, &rq[8 + q]);
             }
             if (MPI_Waitall(16, rq, MPI_STATUSES_IGNORE) != MPI_SUCCESS) status = 1;
             if (reserve(S, S->n + nin)) status = 1;
@@ -361,65 +530,42 @@ __device__ int __gpu_main(int argc, char** argv) {
                     S->v[k] = d[3];
                 }
             for (int q = 0; q < 8; q++) {
-                free(sbuf[q]);
+                free(g->sbuf[q]);
                 free(rbuf[q]);
             }
         }
         // 3. deposit currents (at the new positions), send ghost currents to their owners
-        for (int c = 0; c < cells; c++) {
-            g.jx[c] = 0.0;
-            g.jy[c] = 0.0;
-        }
-        for (int s = 0; s < NSPEC; s++) {
-            Species* S = &sp[s];
-            for (long k = 0; k < S->n; k++) {
-                int i, j;
-                double fx, fy;
-                cic(&g, S->x[k], S->y[k], &i, &j, &fx, &fy);
-                deposit(&g, g.jx, i, j, fx, fy, S->qw * S->u[k]);
-                deposit(&g, g.jy, i, j, fx, fy, S->qw * S->v[k]);
-            }
-        }
-        halo_add(&g, g.jx, sb, rb, left, right, down, up);
-        halo_add(&g, g.jy, sb, rb, left, right, down, up);
+        gpumpi_parallel_for(g->cells, clear_current_cell, g);
+        gpumpi_parallel_for(nchunk, deposit_chunk, g);
+        gpumpi_parallel_for(g->cells, current_from_fixed_cell, g);
+        halo_add(g, g->jx, sb, rb, left, right, down, up);
+        halo_add(g, g->jy, sb, rb, left, right, down, up);
         // 4. fields: Bz half step from E, E full step from Bz and J, Bz second half step
-        for (int pass = 0; pass < 2; pass++) {
-            halo_fill(&g, g.ex, sb, rb, left, right, down, up);
-            halo_fill(&g, g.ey, sb, rb, left, right, down, up);
-            for (int j = 0; j < g.ny; j++)
-                for (int i = 0; i < g.nx; i++) {
-                    const double curl = (g.ey[gid(&g, i + 1, j)] - g.ey[gid(&g, i, j)]) -
-                                        (g.ex[gid(&g, i, j + 1)] - g.ex[gid(&g, i, j)]);
-                    g.bz[gid(&g, i, j)] -= 0.5 * dt * curl;
-                }
-            if (pass == 1) break;
-            halo_fill(&g, g.bz, sb, rb, left, right, down, up);
-            for (int j = 0; j < g.ny; j++)
-                for (int i = 0; i < g.nx; i++) {
-                    const int c = gid(&g, i, j);
-                    g.ex[c] += dt * ((g.bz[c] - g.bz[gid(&g, i, j - 1)]) - g.jx[c]);
-                    g.ey[c] += dt * (-(g.bz[c] - g.bz[gid(&g, i - 1, j)]) - g.jy[c]);
-                }
-        }
+        halo_fill(g, g->ex, sb, rb, left, right, down, up);
+        halo_fill(g, g->ey, sb, rb, left, right, down, up);
+        gpumpi_parallel_for(g->ny, bz_half_row, g);
+        halo_fill(g, g->bz, sb, rb, left, right, down, up);
+        gpumpi_parallel_for(g->ny, e_full_row, g);
+        halo_fill(g, g->ex, sb, rb, left, right, down, up);
+        halo_fill(g, g->ey, sb, rb, left, right, down, up);
+        gpumpi_parallel_for(g->ny, bz_half_row, g);
         // 5. energies
         if (cyc % report == 0 || cyc == cycles) {
-            double e[4] = {0.0, 0.0, 0.0, 0.0}, tot[4];
-            for (int s = 0; s < NSPEC; s++) {
-                Species* S = &sp[s];
-                double ke = 0.0;
-                for (long k = 0; k < S->n; k++) ke += S->u[k] * S->u[k] + S->v[k] * S->v[k];
-                e[s] = 0.5 * S->mw * ke;
+            gpumpi_parallel_for(nchunk, energy_chunk, g);
+            double ke[NSPEC] = {0.0, 0.0}, e[4], tot[4];
+            double fe = 0.0, fb = 0.0;
+            for (int c = 0; c < nchunk; c++) {
+                ke[0] += g->part[c * 4 + 0];
+                ke[1] += g->part[c * 4 + 1];
+                fe += g->part[c * 4 + 2];
+                fb += g->part[c * 4 + 3];
             }
-            for (int j = 0; j < g.ny; j++)
-                for (int i = 0; i < g.nx; i++) {
-                    const int c = gid(&g, i, j);
-                    e[2] += g.ex[c] * g.ex[c] + g.ey[c] * g.ey[c];
-                    e[3] += g.bz[c] * g.bz[c];
-                }
-            e[2] *= 0.5;
-            e[3] *= 0.5;
+            e[0] = 0.5 * g->sp[0].mw * ke[0];
+            e[1] = 0.5 * g->sp[1].mw * ke[1];
+            e[2] = 0.5 * fe;
+            e[3] = 0.5 * fb;
             MPI_Allreduce(e, tot, 4, MPI_DOUBLE, MPI_SUM, MPI_COMM_WORLD);
-            long np = sp[0].n + sp[1].n, npt = 0;
+            long np = g->sp[0].n + g->sp[1].n, npt = 0;
             MPI_Allreduce(&np, &npt, 1, MPI_LONG, MPI_SUM, MPI_COMM_WORLD);
             if (rank == 0)
                 printf("pic cycle %d particles %ld kinetic_e %.17e kinetic_i %.17e electric %.17e magnetic %.17e\n",
@@ -430,10 +576,10 @@ __device__ int __gpu_main(int argc, char** argv) {
     // checksum of every particle's position bits, folded per rank and summed in rank order
     unsigned long long h = 0, hsum = 0;
     for (int s = 0; s < NSPEC; s++)
-        for (long k = 0; k < sp[s].n; k++) {
+        for (long k = 0; k < g->sp[s].n; k++) {
             unsigned long long a, b;
-            memcpy(&a, &sp[s].x[k], 8);
-            memcpy(&b, &sp[s].y[k], 8);
+            memcpy(&a, &g->sp[s].x[k], 8);
+            memcpy(&b, &g->sp[s].y[k], 8);
             h += mix64(a ^ mix64(b));
         }
     MPI_Reduce(&h, &hsum, 1, MPI_UNSIGNED_LONG_LONG, MPI_SUM, 0, MPI_COMM_WORLD);
@@ -446,13 +592,22 @@ __device__ int __gpu_main(int argc, char** argv) {
         printf("pic-time seconds %.6f cycles %d ranks %d (%dx%d)\n", tmax, cycles, size, PX, PY);
     }
     for (int s = 0; s < NSPEC; s++) {
-        free(sp[s].x);
-        free(sp[s].y);
-        free(sp[s].u);
-        free(sp[s].v);
+        free(g->sp[s].x);
+        free(g->sp[s].y);
+        free(g->sp[s].u);
+        free(g->sp[s].v);
+        free(g->sp[s].ax);
+        free(g->sp[s].ay);
+        free(g->sp[s].au);
+        free(g->sp[s].av);
     }
-    free(out_idx);
+    free(g->dest);
+    free(g->ajx);
+    free(g->part);
+    free(g->ccount);
+    free(g->coff);
     free(fields);
+    free(g);
     free(sb);
     free(rb);
     MPI_Finalize();

@@ -138,6 +138,14 @@ struct timezone;
 __device__ int __gpu_gettimeofday(struct timeval* tv, void* tz);
 __device__ time_t __gpu_time(time_t* tloc);
 __device__ clock_t __gpu_clock(void);
+// Parallel loop over the calling rank's thread block (an extension: the
+// reference ran one thread per rank).  body(i, arg) runs once for every i in
+// [0, n), spread over the block's threads in unspecified order; the call
+// returns when all iterations are done.  arg must point to heap or global
+// memory (not to the caller's local variables), and the body must not call
+// MPI.  Host builds of the same program run the loop in order.
+typedef void (*__gpu_loop_body)(long i, void* arg);
+__device__ void __gpu_parallel_for(long n, __gpu_loop_body body, void* arg);
 __device__ int __gpu_omp_get_max_threads(void);
 __device__ int __gpu_omp_get_num_threads(void);
 __device__ int __gpu_omp_get_thread_num(void);
