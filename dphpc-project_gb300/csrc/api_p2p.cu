@@ -236,6 +236,10 @@ static __device__ int start_send(const void* buf, int count, MPI_Datatype dataty
         return MPI_SUCCESS;
     }
     r->peer_world = comm_world_rank(c, dest);
+    if (p2p_send_fast(r)) {   // small eager message: the leader alone, straight from buf
+        *out = r;
+        return MPI_SUCCESS;
+    }
     if (bytes && !is_global(buf)) {
         void* g = heap_alloc(&b.job->heap, bytes);
         if (!g) {
@@ -254,8 +258,11 @@ static __device__ int start_send(const void* buf, int count, MPI_Datatype dataty
     return rc;
 }
 
+// try_fast (blocking receives): a small eager message that is already or
+// soon in the mailbox is taken by the leader alone; otherwise the receive is
+// posted on the block path as usual.
 static __device__ int start_recv(void* buf, int count, MPI_Datatype datatype, int source, int tag,
-                                 MPI_Comm comm, MPI_Request_impl** out) {
+                                 MPI_Comm comm, MPI_Request_impl** out, bool try_fast = false) {
     API_ENTER();
     MPI_Comm_impl* c = comm_resolve(comm);
     if (!c) return MPI_ERR_COMM;
@@ -281,6 +288,18 @@ static __device__ int start_recv(void* buf, int count, MPI_Datatype datatype, in
         r->st_tag = MPI_ANY_TAG;
         *out = r;
         return MPI_SUCCESS;
+    }
+    if (try_fast) {
+        int handled = 0;
+        const int frc = p2p_recv_fast(r, &handled);
+        if (frc) {
+            req_release(r);
+            return frc;
+        }
+        if (handled) {
+            *out = r;
+            return MPI_SUCCESS;
+        }
     }
     if (bytes && !is_global(buf)) {
         void* g = heap_alloc(&b.job->heap, bytes);
@@ -537,7 +556,7 @@ __device__ int MPI_Ssend(const void* buf, int count, MPI_Datatype datatype, int 
 __device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source, int tag,
                         MPI_Comm comm, MPI_Status* status) {
     MPI_Request r = MPI_REQUEST_NULL;
-    int rc = MPI_Irecv(buf, count, datatype, source, tag, comm, &r);
+    int rc = start_recv(buf, count, datatype, source, tag, comm, &r, /*try_fast=*/true);
     if (rc) return rc;
     return MPI_Wait(&r, status);
 }

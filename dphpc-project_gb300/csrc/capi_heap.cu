@@ -257,6 +257,13 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
     out->ops_per_s = ms > 0 ? (double)(cnt[0] + cnt[1]) / (ms / 1000.0) : 0.0;
     out->malloc_cycles_p50 = percentile(hist, 0.50);
     out->malloc_cycles_p99 = percentile(hist, 0.99);
+    if (!cuda_heap) {
+        unsigned st8[8];
+        HK(cudaMemcpy(st8, h.stats, sizeof(st8), cudaMemcpyDeviceToHost));
+        out->fresh_pages = st8[3];
+        out->partial_pops = st8[4];
+        out->partial_full = st8[5];
+    }
 done:
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);

@@ -75,11 +75,48 @@ static __device__ __forceinline__ u64 seg_len(u64 n, int P, int es) {
     return per;
 }
 
-// Copy nb blocks.  src(q)/dst(q)/bytes(q) come from the functor.  Large blocks
-// are copied one after another by the whole block, small ones warp-parallel.
+// Copy nb blocks.  src(q)/dst(q)/bytes(q) come from the functor.  mode 1:
+// blocks one after another, each by the whole thread block; mode 2: one block
+// per warp, warps in parallel; mode 3: thread 0 streams every 16-byte aligned
+// block through the bulk engine in one pipeline while the other threads wait,
+// then all threads copy unaligned blocks and sub-16-byte tails; mode 0: mode 3
+// for blocks of BULK_SEG_MIN and more when the launch has a staging area,
+// else mode 1 for blocks of WARP_COPY_BYTES and more, else mode 2.
 template <class F>
-static __device__ void multi_copy(int nb, int first, u64 avg_bytes, F f, int tid, int T) {
-    if (avg_bytes >= WARP_COPY_BYTES) {
+static __device__ void multi_copy(int nb, int first, u64 avg_bytes, F f, int tid, int T, int mode = 0) {
+    const bool staging = bulk_stage_bytes() >= 8192;
+    if (staging && (mode == 3 || (mode == 0 && avg_bytes >= BULK_SEG_MIN))) {
+        if (tid == 0) {
+            BulkPipe bp;
+            if (bp.begin()) {
+                for (int k = 0; k < nb; k++) {
+                    const void* s;
+                    void* d;
+                    u64 n;
+                    if (!f((first + k) % nb, &s, &d, &n)) continue;
+                    if ((((uintptr_t)s | (uintptr_t)d) & 15) == 0 && n >= 16 && !bp.push((char*)d, (const char*)s, n & ~(u64)15))
+                        break;
+                }
+                bp.finish();
+            }
+        }
+        const int warp = tid >> 5, lane = tid & 31, nw = T >> 5;
+        for (int k = warp; k < nb; k += nw) {
+            const void* s;
+            void* d;
+            u64 n;
+            if (!f((first + k) % nb, &s, &d, &n)) continue;
+            if ((((uintptr_t)s | (uintptr_t)d) & 15) == 0 && n >= 16) {
+                const u64 n16 = n & ~(u64)15;
+                if (n16 < n) warp_copy((char*)d + n16, (const char*)s + n16, n - n16, lane);
+            } else {
+                warp_copy(d, s, n, lane);
+            }
+        }
+        bsync();
+        return;
+    }
+    if (mode == 1 || mode == 3 || (mode == 0 && avg_bytes >= WARP_COPY_BYTES)) {
         for (int k = 0; k < nb; k++) {
             int q = (first + k) % nb;
             const void* s;
@@ -206,12 +243,18 @@ __device__ int coll_allreduce(const CollArgs& a, int tid, int T) {
         raise_flag(cs->depart, me, seq, tid);
         return wait_flags_ge(cs->depart, P, seq, me, tid, T);
     }
-    // Reduce-scatter into the owner's own receive buffer, then allgather by pull.
     const u64 per = seg_len(n, P, es);
     u64 lo = (u64)me * per;
     if (lo > n) lo = n;
     u64 hi = lo + per;
     if (hi > n) hi = n;
+    // Pushing form: fold this rank's segment and write it into every rank's
+    // receive buffer (traffic 2*P*n*s, one synchronisation round).
+    if ((a.algo == 3 || a.algo == 0) && fold_range_push(a.opi, a.dtype, cs->pub, P, lo, hi, tid, T)) {
+        raise_flag(cs->depart, me, seq, tid);
+        return wait_flags_ge(cs->depart, P, seq, me, tid, T);
+    }
+    // Reduce-scatter into the owner's own receive buffer, then allgather by pull.
     if (hi > lo) fold_range(a.opi, a.ufn, a.dtype, a.rsize, (char*)a.rbuf + lo * es, cs->pub, P, 0, lo, hi, tid, T);
     raise_flag(cs->mid, me, seq, tid);
     rc = wait_flags_ge(cs->mid, P, seq, me, tid, T);
@@ -340,7 +383,7 @@ __device__ int coll_allgatherv(const CollArgs& a, int tid, int T) {
         *nb = want < have ? want : have;
         return true;
     };
-    multi_copy(P, me, total * rs / P, blk, tid, T);
+    multi_copy(P, me, total * rs / P, blk, tid, T, a.algo);
     raise_flag(cs->depart, me, seq, tid);
     return wait_flags_ge(cs->depart, P, seq, me, tid, T);
 }
@@ -374,7 +417,7 @@ __device__ int coll_alltoallv(const CollArgs& a, int tid, int T) {
         *nb = want < have ? want : have;
         return *nb > 0;
     };
-    multi_copy(P, me, total * rs / P, blk, tid, T);
+    multi_copy(P, me, total * rs / P, blk, tid, T, a.algo);
     raise_flag(cs->depart, me, seq, tid);
     return wait_flags_ge(cs->depart, P, seq, me, tid, T);
 }

@@ -41,6 +41,9 @@ struct PageMeta {
     u32 slot;       // index of the page in its class list
     u32 pnext;      // partial-stack link: page + 1, 0 = end
     u32 listed;     // 1 while the page is on its class's partial stack
+    u32 nfree;      // free chunks, never below the true count (frees add before
+                    // clearing their bit, claims subtract after setting theirs)
+    u32 pad;
     u64 bits[64];
 };
 static_assert(sizeof(PageMeta) % 8 == 0 && offsetof(PageMeta, bits) % 8 == 0, "64-bit atomics on bits");
@@ -116,8 +119,9 @@ static __device__ __forceinline__ u32 smid() {
 
 // Try to claim up to `want` chunks of class c from page p.
 static __device__ bool claim_in_page(Heap* h, u32 p, int c, int want, int rot, int* w_out,
-                                     u64* m_out) {
+                                     u64* m_out, u32* left = nullptr) {
     PageMeta* pm = &h->meta[p];
+    if (*(volatile u32*)&pm->nfree == 0) return false;   // full: one load instead of a bitmap scan
     const int nw = words_of(c);
     const u64 valid = valid_mask(c);
     for (int k = 0; k < nw; k++) {
@@ -129,6 +133,9 @@ static __device__ bool claim_in_page(Heap* h, u32 p, int c, int want, int rot, i
             u64 old = atomicOr(&pm->bits[w], pick);
             u64 got = pick & ~old;
             if (got) {
+                const u32 k = (u32)__popcll((long long)got);
+                const u32 before = atomicSub(&pm->nfree, k);
+                if (left) *left = before - k;
                 __threadfence();
                 *w_out = w;
                 *m_out = got;
@@ -164,11 +171,15 @@ static __device__ bool claim_batch(Heap* h, int c, int want, u32* page, int* w, 
     for (int tries = 0; tries < 16; tries++) {
         const u32 p = pop_partial(h, c);
         if (p == NO_PAGE) break;
-        if (claim_in_page(h, p, c, want, (int)(stripe % words_of(c)), w, m)) {
+        atomicAdd(&h->stats[4], 1u);
+        u32 left = 0;
+        if (claim_in_page(h, p, c, want, (int)(stripe % words_of(c)), w, m, &left)) {
             *hint = *(volatile u32*)&h->meta[p].slot;   // the window moves to a page with room
+            if (left) push_partial(h, c, p);            // still room: keep it findable
             *page = p;
             return true;
         }
+        atomicAdd(&h->stats[5], 1u);
     }
     // Fresh page from the bump pointer; its bitmap is still all zero.  Claim
     // this group's chunks before the page is published in the class list:
@@ -179,8 +190,11 @@ static __device__ bool claim_batch(Heap* h, int c, int want, u32* page, int* w, 
     if (*(volatile u32*)h->next_page >= h->npages) return false;
     u32 p = atomicAdd(h->next_page, 1u);
     if (p >= h->npages) return false;
+    atomicAdd(&h->stats[3], 1u);
     h->meta[p].cls = (u32)c;
-    if (!claim_in_page(h, p, c, want, 0, w, m)) return false;
+    h->meta[p].nfree = chunks_of(c);
+    u32 left = 0;
+    if (!claim_in_page(h, p, c, want, 0, w, m, &left)) return false;
     __threadfence();
     u32 slot = atomicAdd(&h->cls_count[c], 1u);
     h->meta[p].slot = slot;
@@ -189,6 +203,7 @@ static __device__ bool claim_batch(Heap* h, int c, int want, u32* page, int* w, 
         ((volatile u32*)h->cls_pages)[(u64)c * h->npages + slot] = p;
         *hint = slot;
     }
+    if (left) push_partial(h, c, p);   // other stripes find its room through the stack
     *page = p;
     return true;
 }
@@ -330,7 +345,7 @@ __device__ void* heap_alloc(Heap* h, u64 bytes) {
     if (bytes == 0) bytes = 1;
     if (bytes > (PAGE >> 1)) return large_alloc(h, bytes);
     void* p = small_alloc(h, class_of(bytes));
-    if (p) atomicAdd(&h->stats[0], 1u);
+
     return p;
 }
 
@@ -347,6 +362,7 @@ __device__ void heap_free(Heap* h, void* ptr) {
     if (cls < NCLS) {
         const u64 chunk = (off % PAGE) >> (4 + cls);
         __threadfence();
+        atomicAdd(&pm->nfree, 1u);
         atomicAnd(&pm->bits[chunk / 64], ~(1ull << (chunk % 64)));
         if (*(volatile u32*)&pm->listed == 0u) push_partial(h, (int)cls, p);
         return;
@@ -375,7 +391,8 @@ __device__ u64 heap_usable_size(Heap* h, void* ptr) {
 // Control words of a heap, in one zero-initialised block: the tagged heads of
 // the partial-page stacks, the class page counts, the per-stripe hints, the
 // bump pointer, the free-run list head and lock, and the statistics
-// (0 small allocations, 1 frees of foreign pointers, 2 lock waits that ran out).
+// (1 frees of foreign pointers, 2 lock waits that ran out, 3 fresh small
+// pages, 4 partial-stack pops, 5 pops that found the page full).
 constexpr size_t CTL_PARTIAL = 0;
 constexpr size_t CTL_COUNT = CTL_PARTIAL + sizeof(u64) * NCLS;
 constexpr size_t CTL_HINT = CTL_COUNT + sizeof(u32) * NCLS;

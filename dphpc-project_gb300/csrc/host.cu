@@ -297,6 +297,28 @@ static double now_s() {
 
 // Choose threads per rank: the largest of 256/128/64 that keeps every rank
 // resident, given the kernel's register and shared-memory use.
+size_t pick_rank_smem(const void* kernel, int T, int need) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t stages[] = {65536, 32768, 16384, 8192};
+    for (size_t st : stages) {
+        const size_t smem = rank_smem_bytes(st);
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if ((long long)per * sms >= need) return smem;
+    }
+    return rank_smem_bytes(0);
+}
+
 int choose_threads(const void* kernel, int n, int requested, size_t smem, int* max_resident) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -399,9 +421,8 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         set_last_error("number of ranks must be positive");
         return GPUMPI_EINVAL;
     }
-    const size_t smem = sizeof(BlockCtx) + 64;
     int max_res = 0;
-    int T = choose_threads(kernel, n, o.threads_per_rank, smem, &max_res);
+    int T = choose_threads(kernel, n, o.threads_per_rank, rank_smem_bytes(0), &max_res);
     if (T == 0 || T % 32 || T < 64 || T > 1024) {
         char m[256];
         snprintf(m, sizeof(m),
@@ -413,6 +434,7 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         return GPUMPI_ENORES;
     }
     o.threads_per_rank = T;
+    const size_t smem = pick_rank_smem(kernel, T, n);
     HCHECK(cudaDeviceSetLimit(cudaLimitStackSize, o.stack_bytes));
 
     HostJob hj;

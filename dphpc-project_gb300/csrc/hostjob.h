@@ -31,6 +31,10 @@ size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, cha
 size_t job_footprint(const gpumpi_opts& o, int n);
 int host_job_init(HostJob& hj, cudaStream_t st);
 int choose_threads(const void* kernel, int n, int requested, size_t smem, int* max_resident);
+// Dynamic shared memory for `need` co-resident rank blocks of `kernel` at T
+// threads: BlockCtx plus the largest bulk-copy staging area (64, 32, 16 or
+// 8 KiB, or none) that still lets them all be resident.
+size_t pick_rank_smem(const void* kernel, int T, int need);
 void set_last_error(const char* msg);
 
 // Device image of a program's argv (pointer table + strings, relocated to `dev`).

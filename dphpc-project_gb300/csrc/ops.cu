@@ -184,109 +184,166 @@ template <class T> struct OMinLoc {
 };
 
 // ---------------------------------------------------------------- fold kernels
+// Input q's base (+ in_off): from the block's pointer table in shared memory
+// when fold_range built one, else from the communicator's published table.
 template <class T>
-static __device__ __forceinline__ const T* in_ptr(const Pub* pub, int q, u64 in_off) {
+static __device__ __forceinline__ const T* in_ptr(const Pub* pub, int q, u64 in_off, const char* const* ptab) {
+    if (ptab) return reinterpret_cast<const T*>(ptab[q]);
     return reinterpret_cast<const T*>((const char*)ldcg(&pub[q].sbuf) + in_off);
 }
 
 // Scalar path: any element type, any alignment.
 template <class T, class O>
 static __device__ void fold_scalar(T* out, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
-                                   int tid, int T_) {
+                                   int tid, int T_, const char* const* ptab) {
     for (u64 i = lo + tid; i < hi; i += T_) {
-        T acc = ldcg(in_ptr<T>(pub, 0, in_off) + i);
-        for (int q = 1; q < nin; q++) acc = O::f(ldcg(in_ptr<T>(pub, q, in_off) + i), acc);
+        T acc = ldcg(in_ptr<T>(pub, 0, in_off, ptab) + i);
+        for (int q = 1; q < nin; q++) acc = O::f(ldcg(in_ptr<T>(pub, q, in_off, ptab) + i), acc);
         out[i - lo] = acc;
     }
 }
 
+template <class T, class O>
+static __device__ __forceinline__ void combine(uint4& acc, const uint4& x) {
+    constexpr int V = 16 / sizeof(T);
+    T* a = reinterpret_cast<T*>(&acc);
+    const T* xe = reinterpret_cast<const T*>(&x);
+#pragma unroll
+    for (int e = 0; e < V; e++) a[e] = O::f(xe[e], a[e]);
+}
+
 // 16-byte vector path for 4- and 8-byte element types when every input and
-// the output are 16-byte aligned at element lo.  Four independent vectors per
-// thread keep 64 bytes per thread in flight for every input rank.
+// the output are 16-byte aligned at element lo.
+// With a pointer table in shared memory: one vector per thread at a time and
+// QU input ranks' vectors in flight, folded in rank order.
+// Without one: four independent vectors per thread, each input's base loaded
+// from the communicator's table.
 template <class T, class O>
 static __device__ void fold_vec(T* out, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
-                                int tid, int T_) {
+                                int tid, int T_, const char* const* ptab) {
     constexpr int V = 16 / sizeof(T);
-    constexpr int U = 4;
     const u64 n = hi - lo;
     const u64 nvec = n / V;
     uint4* ov = reinterpret_cast<uint4*>(out);
     u64 v = tid;
-    for (; v + (U - 1) * (u64)T_ < nvec; v += (u64)U * T_) {
-        uint4 acc[U];
-        const uint4* b0 = reinterpret_cast<const uint4*>(in_ptr<T>(pub, 0, in_off) + lo);
+    if (ptab) {
+        constexpr int QU = 8;
+        for (; v < nvec; v += T_) {
+            uint4 acc = __ldcg(reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(ptab[0]) + lo) + v);
+            int q = 1;
+            for (; q + QU <= nin; q += QU) {
+                uint4 x[QU];
 #pragma unroll
-        for (int k = 0; k < U; k++) acc[k] = __ldcg(b0 + v + (u64)k * T_);
-        for (int q = 1; q < nin; q++) {
-            const uint4* bq = reinterpret_cast<const uint4*>(in_ptr<T>(pub, q, in_off) + lo);
-            uint4 x[U];
+                for (int k = 0; k < QU; k++)
+                    x[k] = __ldcg(reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(ptab[q + k]) + lo) + v);
 #pragma unroll
-            for (int k = 0; k < U; k++) x[k] = __ldcg(bq + v + (u64)k * T_);
-#pragma unroll
-            for (int k = 0; k < U; k++) {
-                T* a = reinterpret_cast<T*>(&acc[k]);
-                const T* xe = reinterpret_cast<const T*>(&x[k]);
-#pragma unroll
-                for (int e = 0; e < V; e++) a[e] = O::f(xe[e], a[e]);
+                for (int k = 0; k < QU; k++) combine<T, O>(acc, x[k]);
             }
+            for (; q < nin; q++)
+                combine<T, O>(acc, __ldcg(reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(ptab[q]) + lo) + v));
+            ov[v] = acc;
         }
+    } else {
+        constexpr int U = 4;
+        for (; v + (U - 1) * (u64)T_ < nvec; v += (u64)U * T_) {
+            uint4 acc[U];
+            const uint4* b0 = reinterpret_cast<const uint4*>(in_ptr<T>(pub, 0, in_off, ptab) + lo);
 #pragma unroll
-        for (int k = 0; k < U; k++) ov[v + (u64)k * T_] = acc[k];
-    }
-    for (; v < nvec; v += T_) {
-        uint4 acc = __ldcg(reinterpret_cast<const uint4*>(in_ptr<T>(pub, 0, in_off) + lo) + v);
-        for (int q = 1; q < nin; q++) {
-            uint4 x = __ldcg(reinterpret_cast<const uint4*>(in_ptr<T>(pub, q, in_off) + lo) + v);
-            T* a = reinterpret_cast<T*>(&acc);
-            const T* xe = reinterpret_cast<const T*>(&x);
+            for (int k = 0; k < U; k++) acc[k] = __ldcg(b0 + v + (u64)k * T_);
+            for (int q = 1; q < nin; q++) {
+                const uint4* bq = reinterpret_cast<const uint4*>(in_ptr<T>(pub, q, in_off, ptab) + lo);
+                uint4 x[U];
 #pragma unroll
-            for (int e = 0; e < V; e++) a[e] = O::f(xe[e], a[e]);
+                for (int k = 0; k < U; k++) x[k] = __ldcg(bq + v + (u64)k * T_);
+#pragma unroll
+                for (int k = 0; k < U; k++) combine<T, O>(acc[k], x[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < U; k++) ov[v + (u64)k * T_] = acc[k];
         }
-        ov[v] = acc;
+        for (; v < nvec; v += T_) {
+            uint4 acc = __ldcg(reinterpret_cast<const uint4*>(in_ptr<T>(pub, 0, in_off, ptab) + lo) + v);
+            for (int q = 1; q < nin; q++)
+                combine<T, O>(acc, __ldcg(reinterpret_cast<const uint4*>(in_ptr<T>(pub, q, in_off, ptab) + lo) + v));
+            ov[v] = acc;
+        }
     }
     const u64 done = nvec * V;
-    if (done < n) fold_scalar<T, O>(out + done, pub, nin, in_off, lo + done, hi, tid, T_);
+    if (done < n) fold_scalar<T, O>(out + done, pub, nin, in_off, lo + done, hi, tid, T_, ptab);
+}
+
+// Fold [lo, hi) of every input and write the result at the same place in
+// every output (ptab: inputs, otab: outputs, both in shared memory and 16-byte
+// aligned).  QU input ranks' vectors in flight per thread, folded in rank order.
+template <class T, class O>
+static __device__ __noinline__ void fold_push_t(const char* const* ptab, const char* const* otab, int nin, u64 lo,
+                                                u64 hi, int tid, int T_) {
+    constexpr int V = 16 / sizeof(T);
+    constexpr int QU = 8;
+    const u64 n = hi - lo;
+    const u64 nvec = n / V;
+    for (u64 v = tid; v < nvec; v += T_) {
+        uint4 acc = __ldcg(reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(ptab[0]) + lo) + v);
+        int q = 1;
+        for (; q + QU <= nin; q += QU) {
+            uint4 x[QU];
+#pragma unroll
+            for (int k = 0; k < QU; k++)
+                x[k] = __ldcg(reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(ptab[q + k]) + lo) + v);
+#pragma unroll
+            for (int k = 0; k < QU; k++) combine<T, O>(acc, x[k]);
+        }
+        for (; q < nin; q++)
+            combine<T, O>(acc, __ldcg(reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(ptab[q]) + lo) + v));
+        for (int r = 0; r < nin; r++)
+            reinterpret_cast<uint4*>(const_cast<T*>(reinterpret_cast<const T*>(otab[r]) + lo))[v] = acc;
+    }
+    for (u64 i = lo + nvec * V + tid; i < hi; i += T_) {
+        T acc = ldcg(reinterpret_cast<const T*>(ptab[0]) + i);
+        for (int q = 1; q < nin; q++) acc = O::f(ldcg(reinterpret_cast<const T*>(ptab[q]) + i), acc);
+        for (int r = 0; r < nin; r++) const_cast<T*>(reinterpret_cast<const T*>(otab[r]))[i] = acc;
+    }
 }
 
 // One out-of-line function per (type, operator): each gets its own register
 // allocation instead of sharing one across the whole dispatch switch.
 template <class T, class O>
 static __device__ __noinline__ void fold_t(void* outv, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
-                                           int tid, int T_) {
+                                           int tid, int T_, const char* const* ptab) {
     T* out = reinterpret_cast<T*>(outv);
     if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
         bool aligned = ((uintptr_t)out & 15) == 0;
         for (int q = 0; q < nin && aligned; q++)
-            aligned = (((uintptr_t)(in_ptr<T>(pub, q, in_off) + lo)) & 15) == 0;
+            aligned = (((uintptr_t)(in_ptr<T>(pub, q, in_off, ptab) + lo)) & 15) == 0;
         if (aligned) {
-            fold_vec<T, O>(out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_vec<T, O>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             return;
         }
     }
-    fold_scalar<T, O>(out, pub, nin, in_off, lo, hi, tid, T_);
+    fold_scalar<T, O>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
 }
 
 template <template <class> class O>
 static __device__ void fold_numeric(int canon, void* out, const Pub* pub, int nin, u64 in_off,
-                                    u64 lo, u64 hi, int tid, int T_) {
+                                    u64 lo, u64 hi, int tid, int T_, const char* const* ptab) {
     switch (canon) {
-        case K_I8: fold_t<signed char, O<signed char>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_U8: fold_t<unsigned char, O<unsigned char>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_I16: fold_t<short, O<short>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_U16: fold_t<unsigned short, O<unsigned short>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_I32: fold_t<int, O<int>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_U32: fold_t<unsigned, O<unsigned>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_I64: fold_t<long long, O<long long>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
-        case K_U64: fold_t<unsigned long long, O<unsigned long long>>(out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case K_I8: fold_t<signed char, O<signed char>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_U8: fold_t<unsigned char, O<unsigned char>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_I16: fold_t<short, O<short>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_U16: fold_t<unsigned short, O<unsigned short>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_I32: fold_t<int, O<int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_U32: fold_t<unsigned, O<unsigned>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_I64: fold_t<long long, O<long long>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
+        case K_U64: fold_t<unsigned long long, O<unsigned long long>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
         default: break;
     }
 }
 
 template <template <class> class O>
 static __device__ void fold_float(int canon, void* out, const Pub* pub, int nin, u64 in_off,
-                                  u64 lo, u64 hi, int tid, int T_) {
-    if (canon == K_F32) fold_t<float, O<float>>(out, pub, nin, in_off, lo, hi, tid, T_);
-    else if (canon == K_F64) fold_t<double, O<double>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                                  u64 lo, u64 hi, int tid, int T_, const char* const* ptab) {
+    if (canon == K_F32) fold_t<float, O<float>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+    else if (canon == K_F64) fold_t<double, O<double>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
 }
 
 static __device__ void fold_user(MPI_User_function* fn, MPI_Datatype dt, int es, void* out,
@@ -310,6 +367,57 @@ static __device__ void fold_user(MPI_User_function* fn, MPI_Datatype dt, int es,
     }
 }
 
+template <template <class> class O>
+static __device__ bool fold_push_op(int canon, const char* const* ptab, const char* const* otab, int nin, u64 lo,
+                                    u64 hi, int tid, int T_) {
+    switch (canon) {
+        case K_I32: fold_push_t<int, O<int>>(ptab, otab, nin, lo, hi, tid, T_); return true;
+        case K_U32: fold_push_t<unsigned, O<unsigned>>(ptab, otab, nin, lo, hi, tid, T_); return true;
+        case K_I64: fold_push_t<long long, O<long long>>(ptab, otab, nin, lo, hi, tid, T_); return true;
+        case K_U64: fold_push_t<unsigned long long, O<unsigned long long>>(ptab, otab, nin, lo, hi, tid, T_); return true;
+        case K_F32: fold_push_t<float, O<float>>(ptab, otab, nin, lo, hi, tid, T_); return true;
+        case K_F64: fold_push_t<double, O<double>>(ptab, otab, nin, lo, hi, tid, T_); return true;
+        default: return false;
+    }
+}
+
+static __device__ __forceinline__ bool push_type(int canon) {
+    return canon == K_I32 || canon == K_U32 || canon == K_I64 || canon == K_U64 || canon == K_F32 || canon == K_F64;
+}
+
+// Allreduce, pushing form: this rank folds [lo, hi) of every rank's input in
+// rank order and stores the result into every rank's receive buffer.  Returns
+// false (the same on every rank and every thread, since it depends only on the
+// launch, the operator and the published buffers) when the form does not
+// apply: no staging area for the two pointer tables, a user or bitwise
+// operator, a type that is not 4 or 8 bytes, or a buffer not 16-byte aligned.
+__device__ bool fold_range_push(int opi, MPI_Datatype base, const Pub* pub, int nin, u64 lo, u64 hi, int tid,
+                                int T_) {
+    if (opi < 0 || opi > 3 || nin < 2) return false;
+    const int canon = basic_info((int)base).canon;
+    if (!push_type(canon) || bulk_stage_bytes() < (u32)(2 * nin * sizeof(char*))) return false;
+    extern __shared__ __align__(16) char gm_dsmem[];
+    const char** ptab = reinterpret_cast<const char**>(gm_dsmem + BCTX_BYTES + BULK_BAR_BYTES);
+    const char** otab = ptab + nin;
+    int bad = 0;
+    for (int q = tid; q < nin; q += T_) {
+        ptab[q] = (const char*)ldcg(&pub[q].sbuf);
+        otab[q] = (const char*)ldcg(&pub[q].rbuf);
+        bad |= ((((uintptr_t)ptab[q]) | ((uintptr_t)otab[q])) & 15) != 0;
+    }
+    if (bar_or(bad, T_)) return false;
+    if (hi > lo) {
+        switch (opi) {
+            case 0: fold_push_op<OMax>(canon, ptab, otab, nin, lo, hi, tid, T_); break;
+            case 1: fold_push_op<OMin>(canon, ptab, otab, nin, lo, hi, tid, T_); break;
+            case 2: fold_push_op<OSum>(canon, ptab, otab, nin, lo, hi, tid, T_); break;
+            default: fold_push_op<OProd>(canon, ptab, otab, nin, lo, hi, tid, T_); break;
+        }
+    }
+    bsync();
+    return true;
+}
+
 __device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, int esize, void* out, const Pub* pub, int nin,
                            u64 in_off, u64 lo, u64 hi, int tid, int T_) {
     if (hi <= lo || nin <= 0) {
@@ -322,57 +430,67 @@ __device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, i
         return;
     }
     const int canon = basic_info((int)base).canon;
+    // Input pointers (+ in_off) in the staging area of shared memory, when the
+    // launch gave one: the fold then reads each input's base without a load
+    // through L2.
+    const char** ptab = nullptr;
+    if (nin >= 2 && bulk_stage_bytes() >= (u32)nin * sizeof(char*)) {
+        extern __shared__ __align__(16) char gm_dsmem[];
+        ptab = reinterpret_cast<const char**>(gm_dsmem + BCTX_BYTES + BULK_BAR_BYTES);
+        for (int q = tid; q < nin; q += T_) ptab[q] = (const char*)ldcg(&pub[q].sbuf) + in_off;
+        bsync();
+    }
     switch (opi) {
         case 0:
-            fold_numeric<OMax>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            fold_float<OMax>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OMax>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            fold_float<OMax>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
         case 1:
-            fold_numeric<OMin>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            fold_float<OMin>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OMin>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            fold_float<OMin>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
         case 2:
-            fold_numeric<OSum>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            fold_float<OSum>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_CF32) fold_t<gpumpi_cfloat, OSum<gpumpi_cfloat>>(out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_CF64) fold_t<gpumpi_cdouble, OSum<gpumpi_cdouble>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OSum>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            fold_float<OSum>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_CF32) fold_t<gpumpi_cfloat, OSum<gpumpi_cfloat>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_CF64) fold_t<gpumpi_cdouble, OSum<gpumpi_cdouble>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
         case 3:
-            fold_numeric<OProd>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            fold_float<OProd>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_CF32) fold_t<gpumpi_cfloat, OProd<gpumpi_cfloat>>(out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_CF64) fold_t<gpumpi_cdouble, OProd<gpumpi_cdouble>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OProd>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            fold_float<OProd>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_CF32) fold_t<gpumpi_cfloat, OProd<gpumpi_cfloat>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_CF64) fold_t<gpumpi_cdouble, OProd<gpumpi_cdouble>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
         case 4:
-            fold_numeric<OLAnd>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_BOOL) fold_t<bool, OLAnd<bool>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OLAnd>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_BOOL) fold_t<bool, OLAnd<bool>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
-        case 5: fold_numeric<OBAnd>(canon, out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case 5: fold_numeric<OBAnd>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
         case 6:
-            fold_numeric<OLOr>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_BOOL) fold_t<bool, OLOr<bool>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OLOr>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_BOOL) fold_t<bool, OLOr<bool>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
-        case 7: fold_numeric<OBOr>(canon, out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case 7: fold_numeric<OBOr>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
         case 8:
-            fold_numeric<OLXor>(canon, out, pub, nin, in_off, lo, hi, tid, T_);
-            if (canon == K_BOOL) fold_t<bool, OLXor<bool>>(out, pub, nin, in_off, lo, hi, tid, T_);
+            fold_numeric<OLXor>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+            if (canon == K_BOOL) fold_t<bool, OLXor<bool>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             break;
-        case 9: fold_numeric<OBXor>(canon, out, pub, nin, in_off, lo, hi, tid, T_); break;
+        case 9: fold_numeric<OBXor>(canon, out, pub, nin, in_off, lo, hi, tid, T_, ptab); break;
         case 10:
         case 11: {
             const bool mx = opi == 10;
             if (canon == K_2INT) {
-                if (mx) fold_t<gpumpi_2int, OMaxLoc<gpumpi_2int>>(out, pub, nin, in_off, lo, hi, tid, T_);
-                else fold_t<gpumpi_2int, OMinLoc<gpumpi_2int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                if (mx) fold_t<gpumpi_2int, OMaxLoc<gpumpi_2int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+                else fold_t<gpumpi_2int, OMinLoc<gpumpi_2int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             } else if (canon == K_FLOATINT) {
-                if (mx) fold_t<gpumpi_float_int, OMaxLoc<gpumpi_float_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
-                else fold_t<gpumpi_float_int, OMinLoc<gpumpi_float_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                if (mx) fold_t<gpumpi_float_int, OMaxLoc<gpumpi_float_int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+                else fold_t<gpumpi_float_int, OMinLoc<gpumpi_float_int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             } else if (canon == K_DOUBLEINT) {
-                if (mx) fold_t<gpumpi_double_int, OMaxLoc<gpumpi_double_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
-                else fold_t<gpumpi_double_int, OMinLoc<gpumpi_double_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                if (mx) fold_t<gpumpi_double_int, OMaxLoc<gpumpi_double_int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+                else fold_t<gpumpi_double_int, OMinLoc<gpumpi_double_int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             } else if (canon == K_LONGINT) {
-                if (mx) fold_t<gpumpi_long_int, OMaxLoc<gpumpi_long_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
-                else fold_t<gpumpi_long_int, OMinLoc<gpumpi_long_int>>(out, pub, nin, in_off, lo, hi, tid, T_);
+                if (mx) fold_t<gpumpi_long_int, OMaxLoc<gpumpi_long_int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
+                else fold_t<gpumpi_long_int, OMinLoc<gpumpi_long_int>>(out, pub, nin, in_off, lo, hi, tid, T_, ptab);
             }
             break;
         }

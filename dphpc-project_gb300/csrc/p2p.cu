@@ -43,7 +43,9 @@ static __device__ int claim_and_fill(Job* j, MPI_Request_impl* r) {
         if (freeb == 0) return -1;
         s = __ffsll((long long)freeb) - 1;
         u64 bit = 1ull << s;
-        u64 old = atomicOr(&mb->used, bit);
+        // acquire: a slot freed by the receiver's release of `used` is claimed
+        // only after the receiver's clear of its ready bit
+        u64 old = atom_or_acquire(&mb->used, bit);
         if (!(old & bit)) break;
         used = old | bit;
     }
@@ -85,8 +87,9 @@ static __device__ void deliver_staged(MPI_Request_impl* r, int tid, int T) {
     bsync();
     if (tid == 0) {
         r->state = eager ? RS_DONE : RS_WAIT_RDV;
-        __threadfence();
-        atom_or_release(&b.job->mbox[peer].ready, 1ull << slot);
+        // release: the header and the payload copied by the block (ordered by
+        // the barrier above) become visible before the ready bit
+        red_or_release(&b.job->mbox[peer].ready, 1ull << slot);
     }
 }
 
@@ -213,13 +216,14 @@ static __device__ int progress_recvs(int tid, int T) {
                 r->st_bytes = bytes < r->bytes ? bytes : r->bytes;
                 r->st_err = bytes > r->bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
                 u32* done = kind == 1 ? ldcg(&h->rdv_done) : nullptr;
-                atomicAnd(&mb->ready, ~(1ull << slot));
+                red_and_relaxed(&mb->ready, ~(1ull << slot));
                 if (done) {
                     __threadfence();
                     st_release32(done, 1u);
                 }
-                __threadfence();
-                atomicAnd(&mb->used, ~(1ull << slot));
+                // release: the ready clear and the reads of the slot come before
+                // the slot can be claimed again
+                red_and_release(&mb->used, ~(1ull << slot));
                 r->state = RS_DONE;
                 const int nxt = r->next;
                 if (prev >= 0) p->reqs[prev].next = nxt;
@@ -382,6 +386,110 @@ __device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status*
         if (tid == 0) code = wait_check(t0, did, &ns, "probe timed out");
         code = (int)bcast(code, tid);
         if (code) return code;
+    }
+}
+
+// ---------------------------------------------------------------- leader-only small messages
+// Small eager messages need no block: the leader claims the slot, copies the
+// payload and publishes it (send), or finds the oldest matching message,
+// copies it out and frees the slot (blocking receive), without waking the
+// helper threads.  It reads and writes the user's buffer itself, so a buffer in
+// its local memory needs no staging.  The receive path is taken only when no
+// receive is posted and no send is deferred, so message order and matching
+// are the same as on the block path; anything else (a rendezvous message, a
+// full mailbox) falls back to the block path before touching any state.
+
+static __device__ void leader_copy(void* dst, const void* src, u64 n) {
+    char* d = (char*)dst;
+    const char* s = (const char*)src;
+    if ((((uintptr_t)d | (uintptr_t)s) & 15) == 0) {
+        const u64 nv = n >> 4;
+        for (u64 i = 0; i < nv; i++) ((uint4*)d)[i] = ((const uint4*)s)[i];
+        for (u64 i = nv << 4; i < n; i++) d[i] = s[i];
+    } else if ((((uintptr_t)d | (uintptr_t)s) & 7) == 0) {
+        const u64 nv = n >> 3;
+        for (u64 i = 0; i < nv; i++) ((u64*)d)[i] = ((const u64*)s)[i];
+        for (u64 i = nv << 3; i < n; i++) d[i] = s[i];
+    } else {
+        for (u64 i = 0; i < n; i++) d[i] = s[i];
+    }
+}
+
+// Leader: send r (r->buf may be local memory) without the block.  False: use the block path.
+__device__ bool p2p_send_fast(MPI_Request_impl* r) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    if (r->bytes > FAST_MSG_BYTES || r->bytes > j->eager_bytes || b.priv->defer_head >= 0) return false;
+    r->done = 0;
+    const int slot = claim_and_fill(j, r);
+    if (slot < 0) return false;
+    if (r->bytes) leader_copy(eager_slot(j, r->peer_world, slot), r->buf, r->bytes);
+    red_or_release(&j->mbox[r->peer_world].ready, 1ull << slot);
+    r->state = RS_DONE;
+    return true;
+}
+
+// Leader: blocking receive of a small eager message into r (r->buf may be
+// local memory).  Returns 0 with *handled = 1 when done, 0 with *handled = 0
+// when the block path must take over, or an error code.
+__device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    RankPriv* p = b.priv;
+    *handled = 0;
+    if (p->recv_head >= 0 || p->defer_head >= 0) return MPI_SUCCESS;
+    Mailbox* mb = &j->mbox[b.rank];
+    const u64 t0 = gtime();
+    unsigned ns = 32;
+    for (;;) {
+        u64 ready = ld_acquire(&mb->ready);
+        int best = -1;
+        u64 best_stamp = ~0ull;
+        while (ready) {
+            const int s = __ffsll((long long)ready) - 1;
+            ready &= ready - 1;
+            const MsgHdr* h = &mb->hdr[s];
+            if (__ldcg(&h->ctx) != r->ctx) continue;
+            if (r->peer != MPI_ANY_SOURCE && __ldcg(&h->src) != r->peer) continue;
+            if (r->tag != MPI_ANY_TAG && __ldcg(&h->tag) != r->tag) continue;
+            const u64 st = __ldcg(&h->stamp);
+            if (st < best_stamp) {
+                best_stamp = st;
+                best = s;
+            }
+        }
+        if (best >= 0) {
+            const MsgHdr* h = &mb->hdr[best];
+            const u64 bytes = __ldcg(&h->bytes);
+            if (__ldcg(&h->kind) != 0 || bytes > FAST_MSG_BYTES) return MPI_SUCCESS;   // block path
+            const u64 n = bytes < r->bytes ? bytes : r->bytes;
+            const char* src = eager_slot(j, b.rank, best);
+            if (n) {   // the slot is 16-byte aligned; the destination may not be
+                char* d = (char*)r->buf;
+                u64 i = 0;
+                if (((uintptr_t)d & 15) == 0)
+                    for (; i + 16 <= n; i += 16) *(uint4*)(d + i) = __ldcg((const uint4*)(src + i));
+                else if (((uintptr_t)d & 7) == 0)
+                    for (; i + 8 <= n; i += 8) *(u64*)(d + i) = __ldcg((const u64*)(src + i));
+                for (; i < n; i++) d[i] = __ldcg(src + i);
+            }
+            r->st_source = __ldcg(&h->src);
+            r->st_tag = __ldcg(&h->tag);
+            r->st_bytes = n;
+            r->st_err = bytes > r->bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
+            red_and_relaxed(&mb->ready, ~(1ull << best));
+            red_and_release(&mb->used, ~(1ull << best));
+            r->state = RS_DONE;
+            *handled = 1;
+            return MPI_SUCCESS;
+        }
+        if (job_aborted(j)) return fail_code(j);
+        if (gtime() - t0 > j->timeout_ns) {
+            job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
+            return GPUMPI_ERR_TIMEOUT;
+        }
+        __nanosleep(ns);
+        if (ns < 128) ns <<= 1;
     }
 }
 

@@ -339,6 +339,21 @@ __device__ __forceinline__ u64 atom_or_release(u64* p, u64 v) {
     asm volatile("atom.release.gpu.global.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
     return old;
 }
+__device__ __forceinline__ u64 atom_or_acquire(u64* p, u64 v) {
+    u64 old;
+    asm volatile("atom.acquire.gpu.global.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+// Reductions that return nothing: the issuing thread does not wait for them.
+__device__ __forceinline__ void red_or_release(u64* p, u64 v) {
+    asm volatile("red.release.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_and_relaxed(u64* p, u64 v) {
+    asm volatile("red.relaxed.gpu.global.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_and_release(u64* p, u64 v) {
+    asm volatile("red.release.gpu.global.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ u64 ld_relaxed(const u64* p) {
     u64 v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -446,9 +461,22 @@ struct BlockCtx {
         u64 seq;
     } cv;
     int in_call;                  // leader is inside block_call (helpers busy)
+    int bulk_broken;              // a bulk pipeline failed with loads possibly in flight:
+                                  // its barriers may not be initialised again
 };
 
 static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");
+
+// Dynamic shared memory of a rank block: BlockCtx, then (when the launch
+// gave more) the bulk-copy area: mbarriers, then staging buffers.
+constexpr int BCTX_BYTES = (int)((sizeof(BlockCtx) + 127) / 128 * 128);
+constexpr int BULK_BAR_BYTES = 128;
+constexpr int BULK_STAGES = 4;
+constexpr u64 BULK_MIN_BYTES = 16 * 1024;   // blk_copy: smaller copies use vector loads
+constexpr u64 BULK_SEG_MIN = 4 * 1024;      // multi-segment copies: average segment size for the bulk engine
+__host__ __device__ constexpr size_t rank_smem_bytes(size_t stage) {
+    return (size_t)BCTX_BYTES + (stage ? (size_t)BULK_BAR_BYTES + stage : 0);
+}
 
 __device__ __forceinline__ BlockCtx& bctx() {
     extern __shared__ __align__(16) char gm_dsmem[];
@@ -489,6 +517,27 @@ __device__ int wait_u32_nonzero(const volatile u32* addr);
 // ----------------------------------------------------------------- copies
 // Block-cooperative copy of n bytes between global buffers.
 __device__ void blk_copy(void* dst, const void* src, u64 n, int tid, int T);
+
+// ---- bulk asynchronous copies (cp.async.bulk global -> shared -> global) ----
+// One thread drives a ring of BULK_STAGES staging buffers: a chunk is loaded
+// with cp.async.bulk into a stage (completion counted on the stage's
+// mbarrier), then stored from the stage with a bulk store; up to BULK_STAGES
+// loads are in flight while stores drain asynchronously.  Addresses and sizes
+// must be multiples of 16 bytes.  Every wait is bounded by the job timeout.
+__device__ u32 bulk_stage_bytes();     // staging bytes of this block (0: none)
+struct BulkPipe {
+    char* stage;
+    u64* bars;
+    u32 chunk;                 // bytes per stage
+    u64 issued, stored;        // chunk counters
+    char* dst_of[BULK_STAGES];
+    u32 len_of[BULK_STAGES];
+    int err;
+    __device__ bool begin();                  // false: no staging area
+    __device__ bool push(char* dst, const char* src, u64 n);   // queue a 16-byte aligned span
+    __device__ int finish();                  // all stores complete; 0 or an error code
+    __device__ bool retire();
+};
 __device__ void blk_memset(void* dst, int c, u64 n, int tid, int T);
 // Same, using only the 32 lanes of one warp.
 __device__ void warp_copy(void* dst, const void* src, u64 n, int lane);
@@ -515,11 +564,16 @@ __device__ int op_check(MPI_Op op, MPI_Datatype t);
 struct Pub;
 // Rank-order fold of elements [lo, hi): out[i - lo] = acc with acc = in_0[i];
 // acc = op(in_q[i], acc) for q = 1..nin-1, where in_q = pub[q].sbuf + in_off bytes.
+__device__ bool fold_range_push(int opi, MPI_Datatype base, const Pub* pub, int nin, u64 lo, u64 hi, int tid,
+                                int T);
 __device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, int esize, void* out, const Pub* pub, int nin,
                            u64 in_off, u64 lo, u64 hi, int tid, int T);
 
 // p2p engine (block-cooperative)
 __device__ int p2p_send_start(MPI_Request_impl* r, int tid, int T);
+constexpr u64 FAST_MSG_BYTES = 1024;   // eager messages the leader moves alone
+__device__ bool p2p_send_fast(MPI_Request_impl* r);
+__device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled);
 __device__ int p2p_recv_post(MPI_Request_impl* r, int tid, int T);
 __device__ int p2p_progress(int tid, int T, int* did_work);
 __device__ int p2p_wait(MPI_Request_impl* r, int tid, int T, int blocking);

@@ -148,8 +148,123 @@ static __device__ __forceinline__ void copy_range(char* d, const char* s, u64 n,
     }
 }
 
+// ---------------------------------------------------------------- bulk engine
+static __device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+__device__ u32 bulk_stage_bytes() {
+    u32 dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const u32 base = BCTX_BYTES + BULK_BAR_BYTES;
+    return dyn > base ? dyn - base : 0;
+}
+
+__device__ bool BulkPipe::begin() {
+    const u32 bytes = bulk_stage_bytes();
+    chunk = (bytes / BULK_STAGES) & ~15u;
+    if (chunk < 2048 || bctx().bulk_broken) return false;
+    extern __shared__ __align__(16) char gm_dsmem[];
+    bars = reinterpret_cast<u64*>(gm_dsmem + BCTX_BYTES);
+    stage = gm_dsmem + BCTX_BYTES + BULK_BAR_BYTES;
+    issued = stored = 0;
+    err = 0;
+    for (int s = 0; s < BULK_STAGES; s++)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])) : "memory");
+    // the barriers are used by the async proxy; data the bulk loads read was
+    // written (and acquired) through the generic proxy
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    return true;
+}
+
+// Wait for the oldest loaded chunk and start its store.
+__device__ bool BulkPipe::retire() {
+    const int s = (int)(stored % BULK_STAGES);
+    const u32 parity = (u32)((stored / BULK_STAGES) & 1);
+    const u32 bar = smem_u32(&bars[s]);
+    u32 done = 0;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (!done) {
+        Job* j = bctx().job;
+        const u64 t0 = gtime();
+        while (!done) {
+            asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                         : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+            if (!done && gtime() - t0 > j->timeout_ns) {
+                job_fail(j, bctx().rank, GPUMPI_ERR_TIMEOUT, "bulk copy did not complete");
+                err = GPUMPI_ERR_TIMEOUT;
+                return false;
+            }
+        }
+    }
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                 ::"l"(dst_of[s]), "r"(smem_u32(stage + (u64)s * chunk)), "r"(len_of[s]) : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    stored++;
+    return true;
+}
+
+__device__ bool BulkPipe::push(char* dst, const char* src, u64 n) {
+    while (n > 0 && !err) {
+        const u32 len = n < chunk ? (u32)n : chunk;
+        if (issued - stored == BULK_STAGES && !retire()) return false;
+        // the stage is free once the store that last used it has read it
+        if (issued >= BULK_STAGES) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        const int s = (int)(issued % BULK_STAGES);
+        const u32 bar = smem_u32(&bars[s]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(len) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(stage + (u64)s * chunk)), "l"(src), "r"(len), "r"(bar) : "memory");
+        dst_of[s] = dst;
+        len_of[s] = len;
+        issued++;
+        dst += len;
+        src += len;
+        n -= len;
+    }
+    return !err;
+}
+
+__device__ int BulkPipe::finish() {
+    while (stored < issued && retire()) {
+    }
+    // The stores issued so far are waited for in every case.
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    if (err) {
+        // loads may still be in flight: the barriers stay as they are and this
+        // block copies with vector loads from now on
+        bctx().bulk_broken = 1;
+        return err;
+    }
+    // every load completed: retire the barriers, so that the next pipeline may
+    // initialise this memory again (mbarrier.init on a live barrier is undefined)
+    for (int s = 0; s < BULK_STAGES; s++)
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[s])) : "memory");
+    return err;
+}
+
+// Large aligned copies go through the bulk engine, driven by thread 0 (the
+// other threads only copy the unaligned tail); the block synchronises after.
 __device__ void blk_copy(void* dst, const void* src, u64 n, int tid, int T) {
     if (n == 0 || dst == src) return;
+    if (n >= BULK_MIN_BYTES && (((uintptr_t)dst | (uintptr_t)src) & 15) == 0 && bulk_stage_bytes() >= 8192 &&
+        bctx().job != nullptr) {
+        const u64 n16 = n & ~(u64)15;
+        if (tid == 0) {
+            BulkPipe bp;
+            if (bp.begin()) {
+                bp.push((char*)dst, (const char*)src, n16);
+                bp.finish();
+            } else {
+                copy_range((char*)dst, (const char*)src, n16, 0, 1);
+            }
+        }
+        if (n16 < n) copy_range((char*)dst + n16, (const char*)src + n16, n - n16, (u64)tid, (u64)T);
+        bsync();
+        return;
+    }
     copy_range((char*)dst, (const char*)src, n, (u64)tid, (u64)T);
 }
 
@@ -336,6 +451,7 @@ __device__ bool program_block_begin(const Launch& L) {
             b.T = (int)blockDim.x;
             b.leader_mode = 1;
             b.in_call = 0;
+            b.bulk_broken = 0;
             b.call.op = -1;
         }
     }

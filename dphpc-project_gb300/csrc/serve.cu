@@ -121,13 +121,16 @@ extern "C" int gpumpi_serve(const void* kernel, const gpumpi_job_spec* jobs, int
         set_last_error("gpumpi_serve: threads_per_rank must be 64..1024, a multiple of 32");
         return GPUMPI_EINVAL;
     }
-    const size_t smem = sizeof(BlockCtx) + 64;
     int dev = 0, sms = 0, per = 0;
     SCHECK(cudaGetDevice(&dev));
     SCHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem));
+    SCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, rank_smem_bytes(0)));
     int capacity = per * sms;
     if (capacity > 1024) capacity = 1024;
+    // every rank that may run at once keeps its staging area: size it for the capacity
+    const size_t smem = pick_rank_smem(kernel, T, so.max_slots > 0 && so.max_slots < capacity ? so.max_slots : capacity);
+    SCHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem));
+    if (per * sms < capacity) capacity = per * sms;
     const int max_slots = so.max_slots > 0 && so.max_slots < capacity ? so.max_slots : capacity;
     size_t pool_bytes = so.pool_bytes;
     if (pool_bytes == 0) {

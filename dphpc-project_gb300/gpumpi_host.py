@@ -80,7 +80,8 @@ class ChurnStats(ctypes.Structure):
     _fields_ = [("allocs", ctypes.c_uint64), ("frees", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("corrupt", ctypes.c_uint64), ("misaligned", ctypes.c_uint64), ("seconds", ctypes.c_double),
                 ("ops_per_s", ctypes.c_double), ("malloc_cycles_p50", ctypes.c_uint64),
-                ("malloc_cycles_p99", ctypes.c_uint64)]
+                ("malloc_cycles_p99", ctypes.c_uint64), ("fresh_pages", ctypes.c_uint64),
+                ("partial_pops", ctypes.c_uint64), ("partial_full", ctypes.c_uint64)]
 
 
 def malloc_churn(lib: ctypes.CDLL, blocks: int, threads: int, iters: int, live: int = 8, seed: int = 1,
