@@ -233,6 +233,8 @@ def main():
     ap.add_argument("--cpu-lg", type=int, default=16)
     ap.add_argument("--cpu-iters", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="built-in schedules, --threads for every launch")
+    ap.add_argument("--tune-reps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -258,8 +260,25 @@ def main():
     stream = torch.cuda.Stream()
     peak, peak_kind = load_peaks()
 
-    # batched form, graph-captured
+    # batched form, graph-captured; schedules and thread counts from the autotuner
+    # (it times candidates on these buffers before the timed region)
     plan, comms, keep, bufs, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, args.threads)
+    tuning = None
+    plain_threads = plain_algos = None
+    threads = args.threads
+    if not args.no_tune:
+        plan.close()
+        t0 = time.perf_counter()
+        threads, plain_threads, plain_algos = coll.autotune(lib, descs, reps=args.tune_reps)
+        tune_s = time.perf_counter() - t0
+        names = {coll.COLL_BCAST: "bcast", coll.COLL_ALLREDUCE: "allreduce", coll.COLL_ALLTOALL: "alltoall"}
+        algos = {}
+        for d in descs:
+            algos.setdefault(names[d.op], {}).setdefault(str(d.algo), 0)
+            algos[names[d.op]][str(d.algo)] += 1
+        tuning = {"batched_threads": threads, "algo_counts": algos, "seconds": round(tune_s, 2),
+                  "plain_threads_counts": {str(t): plain_threads.count(t) for t in sorted(set(plain_threads))}}
+        plan = coll.Plan(lib, descs, threads=threads, batched=True)
     plan.capture(stream.cuda_stream)
     launches0 = lib.gpumpi_kernel_launches()
     with torch.cuda.stream(stream):
@@ -281,18 +300,30 @@ def main():
     value = nbytes * args.steps * world / secs / 1e9
     kernel_gbs = nbytes / per_step / 1e9
 
-    # plain form on the same buffers
-    plain = coll.Plan(lib, descs, threads=args.threads, batched=False)
+    # plain form on the same buffers: one launch per call and communicator, first
+    # with the batched launch's schedules and threads per rank (the launch
+    # structure is the only difference), then with each launch's own tuned
+    # schedule and thread count (a small communicator may use 1024 threads per rank)
+    plain = coll.Plan(lib, descs, threads=threads, batched=False)
     psecs = time_plan(torch, plain, args.plain_steps, 1, stream)
     plain_gbs = nbytes * args.plain_steps / psecs / 1e9
     plain.close()
+    plain_tuned_gbs = None
+    if plain_threads:
+        pdescs = [type(d).from_buffer_copy(d) for d in descs]
+        for d, a in zip(pdescs, plain_algos):
+            d.algo = a
+        plain = coll.Plan(lib, pdescs, threads=threads, batched=False, plain_threads=plain_threads)
+        psecs = time_plan(torch, plain, args.plain_steps, 1, stream)
+        plain_tuned_gbs = nbytes * args.plain_steps / psecs / 1e9
+        plain.close()
     plan.close()
     del bufs
     torch.cuda.empty_cache()
 
     # end to end through the host-buffer entry point (smaller per-rank count)
     ne = 1 << args.e2e_lg
-    eplan, ecomms, ekeep, ebufs, edescs = build_plan(coll, lib, torch, COMM_SIZES, ne, True, args.threads,
+    eplan, ecomms, ekeep, ebufs, edescs = build_plan(coll, lib, torch, COMM_SIZES, ne, True, threads,
                                                      seed=2)
     sizes_by_comm = {c.h.value: c.n for c in ecomms}
     layout = []
@@ -350,11 +381,15 @@ def main():
             "dtype": "int32+f64",
             "data": "synthetic (seeded uniform int32 [-2^20,2^20), fp64 [-1,1))",
             "config": {"workload": WORKLOAD, "elements_per_rank": n, "comm_sizes": COMM_SIZES,
-                       "threads_per_rank": args.threads, "form": "batched, CUDA graph replay",
+                       "threads_per_rank": threads, "form": "batched, CUDA graph replay",
+                       "tuning": tuning,
                        "l2": "inputs larger than L2 (each step touches ~%.0f GB)" % (nbytes / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "plain": {"value": round(plain_gbs, 2), "unit": "GB/s", "launches_per_step": len(descs),
-                      "batched_over_plain": round(value / world / plain_gbs, 2)},
+                      "batched_over_plain": round(value / world / plain_gbs, 2),
+                      "threads_per_rank": threads,
+                      "tuned_value": round(plain_tuned_gbs, 2) if plain_tuned_gbs else None,
+                      "batched_over_tuned_plain": round(value / world / plain_tuned_gbs, 2) if plain_tuned_gbs else None},
             "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind,
                          "traffic": int(NCU_TRAFFIC_BYTES_2_15 * n / (1 << 15)),

@@ -109,6 +109,7 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_plan_kernel(PlanArgs A
         b.T = (int)blockDim.x;
         b.leader_mode = 0;
         b.in_call = 0;
+        b.bulk_broken = 0;
     }
     __syncthreads();
     MPI_Comm_impl* comm = &A.comms[c].handles[rank];
@@ -140,6 +141,8 @@ struct gpumpi_plan_s {
     PlanArgs batch_args;              // batched launch
     std::vector<PlanArgs> plain_args; // one per descriptor
     std::vector<int> plain_grid;
+    std::vector<int> plain_threads;   // threads per rank of each plain launch
+    std::vector<size_t> plain_smem;   // dynamic shared memory of each plain launch
     int total_slots;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -171,6 +174,10 @@ ApiJob g_api;
 
 int api_job() {
     if (g_api.djob) return GPUMPI_OK;
+    // the plan kernel streams through L2 (ld.global.cg) and stages bulk copies
+    // in shared memory: prefer the largest shared-memory carve-out
+    CK(cudaFuncSetAttribute((const void*)gpumpi_plan_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                            (int)cudaSharedmemCarveoutMaxShared));
     Job hj;
     memset(&hj, 0, sizeof(hj));
     char* mem = nullptr;
@@ -295,9 +302,18 @@ extern "C" int gpumpi_comm_size(gpumpi_comm_t c, int* n) {
 
 extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int threads, int batched,
                                   gpumpi_plan_t* out) {
+    return gpumpi_plan_create_ex(descs, ndesc, threads, batched, nullptr, out);
+}
+
+extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, int threads, int batched,
+                                     const int* plain_threads, gpumpi_plan_t* out) {
     if (!descs || ndesc <= 0 || !out) return GPUMPI_EINVAL;
     if (threads == 0) threads = 128;
     if (threads < 64 || threads > 1024 || threads % 32) return GPUMPI_EINVAL;
+    for (int i = 0; plain_threads && i < ndesc; i++) {
+        const int t = plain_threads[i];
+        if (t != 0 && (t < 64 || t > 1024 || t % 32)) return GPUMPI_EINVAL;
+    }
     int rc = api_job();
     if (rc) return rc;
     // communicators in order of first use; descriptors grouped by communicator, order kept
@@ -310,6 +326,7 @@ extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int 
             return GPUMPI_EINVAL;
         if ((d.op == GPUMPI_COLL_BCAST || d.op == GPUMPI_COLL_REDUCE) && (d.root < 0 || d.root >= d.comm->n))
             return GPUMPI_EINVAL;
+        if (d.algo < 0 || d.algo > 3) return GPUMPI_EINVAL;
         auto it = std::find(comms.begin(), comms.end(), d.comm);
         cidx[i] = (int)(it - comms.begin());
         if (it == comms.end()) comms.push_back(d.comm);
@@ -357,7 +374,7 @@ extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int 
         x.count = d.count;
         x.comm = cidx[i];
         x.esize = esize_of(d.dtype);
-        x.algo = 0;
+        x.algo = d.algo;
         x.sbufs = (void**)(base + off_ptr + sizeof(void*) * pk);
         for (int r = 0; r < P; r++) hp[pk++] = d.sendbufs ? d.sendbufs[r] : nullptr;
         x.rbufs = (void**)(base + off_ptr + sizeof(void*) * pk);
@@ -390,7 +407,7 @@ extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int 
     p->ncomm = ncomm;
     p->batched = batched;
     p->threads = threads;
-    p->smem = sizeof(BlockCtx) + 64;
+    p->smem = rank_smem_bytes(0);
     p->total_slots = total_slots;
     p->batch_args.job = g_api.djob;
     p->batch_args.descs = (const DevDesc*)(base + off_desc);
@@ -400,7 +417,10 @@ extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int 
     p->batch_args.comms = (const DevComm*)(base + off_cm);
     p->plain_args.resize(ndesc);
     p->plain_grid.resize(ndesc);
+    p->plain_threads.resize(ndesc);
     for (int k = 0; k < ndesc; k++) {
+        const int t = plain_threads ? plain_threads[order[k]] : 0;
+        p->plain_threads[k] = t ? t : threads;
         PlanArgs& a = p->plain_args[k];
         a.job = g_api.djob;
         a.descs = (const DevDesc*)(base + off_desc) + k;
@@ -414,16 +434,26 @@ extern "C" int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int 
     int per = 0, sms = 0, dev = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)gpumpi_plan_kernel, threads, p->smem));
-    int need = batched ? total_slots : *std::max_element(p->plain_grid.begin(), p->plain_grid.end());
-    if ((long long)per * sms < need) {
-        char m[200];
-        snprintf(m, sizeof(m), "%d rank blocks of %d threads cannot be co-resident (max %d)", need, threads,
-                 per * sms);
-        set_last_error(m);
-        cudaFree(p->base);
-        delete p;
-        return GPUMPI_ENORES;
+    p->plain_smem.assign(ndesc, rank_smem_bytes(0));
+    for (int k = 0; k <= ndesc; k++) {
+        // k < ndesc: each plain launch at its own thread count; k == ndesc: the batched launch
+        if (k < ndesc && batched) continue;
+        if (k == ndesc && !batched) break;
+        const int t = k < ndesc ? p->plain_threads[k] : threads;
+        const int need = k < ndesc ? p->plain_grid[k] : total_slots;
+        const size_t smem = pick_rank_smem((const void*)gpumpi_plan_kernel, t, need);
+        if (k < ndesc) p->plain_smem[k] = smem;
+        else p->smem = smem;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)gpumpi_plan_kernel, t, smem));
+        if ((long long)per * sms < need) {
+            char m[200];
+            snprintf(m, sizeof(m), "%d rank blocks of %d threads cannot be co-resident (max %d)", need, t,
+                     per * sms);
+            set_last_error(m);
+            cudaFree(p->base);
+            delete p;
+            return GPUMPI_ENORES;
+        }
     }
     *out = p;
     return GPUMPI_OK;
@@ -433,7 +463,7 @@ static int plan_enqueue(gpumpi_plan_t p, cudaStream_t st) {
     const void* k = (const void*)gpumpi_plan_kernel;
     if (p->batched) return launch(k, p->total_slots, p->threads, p->smem, &p->batch_args, st);
     for (int i = 0; i < p->ndesc; i++) {
-        int rc = launch(k, p->plain_grid[i], p->threads, p->smem, &p->plain_args[i], st);
+        int rc = launch(k, p->plain_grid[i], p->plain_threads[i], p->plain_smem[i], &p->plain_args[i], st);
         if (rc) return rc;
     }
     return GPUMPI_OK;
@@ -474,40 +504,120 @@ extern "C" int gpumpi_plan_capture(gpumpi_plan_t p, void* stream) {
 // plan, copy every rank's result back.  host_send/host_recv hold, for each
 // descriptor in the order given to gpumpi_plan_create, one host pointer per
 // rank (nullptr = skip).
+namespace {
+
+// Copies of one direction, merged while both sides continue where the
+// previous copy ended, within one descriptor, the device side inside one
+// allocation (cuMemGetAddressRange, fetched through the runtime) and the host
+// side of one memory type; rank buffers carved from one allocation on each
+// side become one cudaMemcpyAsync.
+typedef int (*AddrRangeFn)(unsigned long long* base, size_t* size, unsigned long long ptr);
+
+AddrRangeFn addr_range() {
+    static AddrRangeFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (AddrRangeFn)f;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+int host_kind(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return (int)a.type;
+}
+
+struct CopyRun {
+    char* dst = nullptr;
+    const char* src = nullptr;
+    size_t n = 0;
+    int desc = -1;
+    unsigned long long dev_end = 0;   // end of the device allocation of the run
+    int hkind = -1;
+    int add(int d_idx, void* d, const void* s, size_t len, cudaMemcpyKind kind, cudaStream_t st) {
+        const bool to_dev = kind == cudaMemcpyHostToDevice;
+        const unsigned long long dptr = (unsigned long long)(to_dev ? (uintptr_t)d : (uintptr_t)s);
+        const void* hptr = to_dev ? s : (const void*)d;
+        if (n && d_idx == desc && (char*)d == dst + n && (const char*)s == src + n && dptr + len <= dev_end &&
+            hkind >= 0 && host_kind(hptr) == hkind) {
+            n += len;
+            return GPUMPI_OK;
+        }
+        int rc = flush(kind, st);
+        dst = (char*)d;
+        src = (const char*)s;
+        n = len;
+        desc = d_idx;
+        dev_end = 0;
+        hkind = -1;
+        unsigned long long base = 0;
+        size_t size = 0;
+        AddrRangeFn f = addr_range();
+        if (f && f(&base, &size, dptr) == 0) {
+            dev_end = base + size;
+            hkind = host_kind(hptr);
+        }
+        return rc;
+    }
+    int flush(cudaMemcpyKind kind, cudaStream_t st) {
+        if (n) CK(cudaMemcpyAsync(dst, src, n, kind, st));
+        n = 0;
+        return GPUMPI_OK;
+    }
+};
+
+}  // namespace
+
 extern "C" int gpumpi_plan_run_host(gpumpi_plan_t p, void* const* host_send, void* const* host_recv,
                                     void* stream, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
     if (!p) return GPUMPI_EINVAL;
     cudaStream_t st = (cudaStream_t)stream;
     size_t k = 0, bi = 0, bo = 0;
-    for (int d = 0; d < p->ndesc; d++) {
+    CopyRun run;
+    int rc = GPUMPI_OK;
+    for (int d = 0; d < p->ndesc && !rc; d++) {
         const int P = p->descs[d].comm->n;
         size_t in, out;
         desc_bytes(p->descs[d], P, &in, &out);
-        for (int r = 0; r < P; r++, k++) {
+        for (int r = 0; r < P && !rc; r++, k++) {
             const bool is_bcast = p->descs[d].op == GPUMPI_COLL_BCAST;
             void* dst = is_bcast ? p->rb[d][r] : p->sb[d][r];
             if (is_bcast && r != p->descs[d].root) continue;
             if (host_send && host_send[k] && dst && in) {
-                CK(cudaMemcpyAsync(dst, host_send[k], in, cudaMemcpyHostToDevice, st));
+                rc = run.add(d, dst, host_send[k], in, cudaMemcpyHostToDevice, st);
                 bi += in;
             }
         }
     }
-    int rc = gpumpi_plan_launch(p, stream);
+    if (!rc) rc = run.flush(cudaMemcpyHostToDevice, st);
+    if (!rc) rc = gpumpi_plan_launch(p, stream);
     if (rc) return rc;
     k = 0;
-    for (int d = 0; d < p->ndesc; d++) {
+    for (int d = 0; d < p->ndesc && !rc; d++) {
         const int P = p->descs[d].comm->n;
         size_t in, out;
         desc_bytes(p->descs[d], P, &in, &out);
-        for (int r = 0; r < P; r++, k++) {
+        for (int r = 0; r < P && !rc; r++, k++) {
             if (p->descs[d].op == GPUMPI_COLL_REDUCE && r != p->descs[d].root) continue;
             if (host_recv && host_recv[k] && p->rb[d][r] && out) {
-                CK(cudaMemcpyAsync(host_recv[k], p->rb[d][r], out, cudaMemcpyDeviceToHost, st));
+                rc = run.add(d, host_recv[k], p->rb[d][r], out, cudaMemcpyDeviceToHost, st);
                 bo += out;
             }
         }
     }
+    if (!rc) rc = run.flush(cudaMemcpyDeviceToHost, st);
+    if (rc) return rc;
     if (h2d_bytes) *h2d_bytes = bi;
     if (d2h_bytes) *d2h_bytes = bo;
     return GPUMPI_OK;

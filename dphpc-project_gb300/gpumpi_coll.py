@@ -23,6 +23,8 @@ class Desc(ctypes.Structure):
         ("count", c_uint64),
         ("sendbufs", POINTER(c_void_p)),
         ("recvbufs", POINTER(c_void_p)),
+        ("algo", c_int),
+        ("pad", c_int),
     ]
 
 
@@ -30,6 +32,8 @@ def bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.gpumpi_comm_create.argtypes = [c_int, POINTER(c_void_p)]
     lib.gpumpi_comm_destroy.argtypes = [c_void_p]
     lib.gpumpi_plan_create.argtypes = [POINTER(Desc), c_int, c_int, c_int, POINTER(c_void_p)]
+    lib.gpumpi_plan_create_ex.argtypes = [POINTER(Desc), c_int, c_int, c_int, POINTER(c_int), POINTER(c_void_p)]
+    lib.gpumpi_autotune.argtypes = [POINTER(Desc), c_int, c_void_p, POINTER(c_int), POINTER(c_int), POINTER(c_int)]
     lib.gpumpi_plan_launch.argtypes = [c_void_p, c_void_p]
     lib.gpumpi_plan_capture.argtypes = [c_void_p, c_void_p]
     lib.gpumpi_plan_run_host.argtypes = [c_void_p, POINTER(c_void_p), POINTER(c_void_p), c_void_p,
@@ -68,24 +72,46 @@ def ptr_array(ptrs):
 
 
 def make_desc(comm: Comm, op: int, dtype: str, count: int, send_ptrs=None, recv_ptrs=None,
-              redop: int = OP_SUM, root: int = 0, keep: list | None = None) -> Desc:
+              redop: int = OP_SUM, root: int = 0, keep: list | None = None, algo: int = 0) -> Desc:
     s = ptr_array(send_ptrs) if send_ptrs is not None else None
     r = ptr_array(recv_ptrs) if recv_ptrs is not None else None
     if keep is not None:
         keep.extend([s, r])
     return Desc(comm.h, op, DT[dtype], redop, root, count,
                 ctypes.cast(s, POINTER(c_void_p)) if s is not None else None,
-                ctypes.cast(r, POINTER(c_void_p)) if r is not None else None)
+                ctypes.cast(r, POINTER(c_void_p)) if r is not None else None, algo, 0)
+
+
+class TuneOpts(ctypes.Structure):
+    _fields_ = [("reps", c_int), ("cache_path", ctypes.c_char_p), ("verbose", c_int)]
+
+
+def autotune(lib, descs: list, reps: int = 5, cache_path: str | None = None, verbose: bool = False):
+    """gpumpi_autotune: sets every descriptor's algo (the batched choice) in
+    place; returns (threads per rank of the batched launch, per-descriptor
+    plain-form threads, per-descriptor plain-form algos)."""
+    arr = (Desc * len(descs))(*descs)
+    plain = (c_int * len(descs))()
+    palgo = (c_int * len(descs))()
+    bt = c_int(0)
+    opts = TuneOpts(reps, cache_path.encode() if cache_path else None, 1 if verbose else 0)
+    check(lib, lib.gpumpi_autotune(arr, len(descs), ctypes.byref(opts), ctypes.byref(bt), plain, palgo),
+          "gpumpi_autotune")
+    for i, d in enumerate(descs):
+        d.algo = arr[i].algo
+    return bt.value, list(plain), list(palgo)
 
 
 class Plan:
-    def __init__(self, lib, descs: list[Desc], threads: int = 128, batched: bool = True):
+    def __init__(self, lib, descs: list[Desc], threads: int = 128, batched: bool = True,
+                 plain_threads: list | None = None):
         self.lib = lib
         arr = (Desc * len(descs))(*descs)
         self._arr = arr
+        pt = (c_int * len(descs))(*plain_threads) if plain_threads else None
         h = c_void_p()
-        check(lib, lib.gpumpi_plan_create(arr, len(descs), threads, 1 if batched else 0, ctypes.byref(h)),
-              "gpumpi_plan_create")
+        check(lib, lib.gpumpi_plan_create_ex(arr, len(descs), threads, 1 if batched else 0, pt, ctypes.byref(h)),
+              "gpumpi_plan_create_ex")
         self.h = h
 
     def launch(self, stream: int = 0):

@@ -148,7 +148,14 @@ typedef struct gpumpi_comm_s* gpumpi_comm_t;
 /* One collective call over one communicator.  sendbufs/recvbufs are host
  * arrays of nranks device pointers (rank r's buffers).  count is elements per
  * rank: the broadcast length, the reduction length, or for ALLTOALL the block
- * sent to each peer. */
+ * sent to each peer.  algo selects the schedule (0 = by message size):
+ *   REDUCE     1 root folds all inputs, 2 every rank folds a segment
+ *   ALLREDUCE  1 every rank folds all inputs, 2 reduce-scatter + allgather,
+ *              3 every rank folds its segment and writes it to every rank
+ *   ALLTOALL, ALLGATHER  1 peer blocks one after another by the whole rank
+ *              block, 2 one peer block per warp, 3 all peer blocks through
+ *              one bulk asynchronous copy pipeline (cp.async.bulk)
+ * gpumpi_autotune fills it in. */
 typedef struct gpumpi_coll_desc {
     gpumpi_comm_t comm;
     int op;
@@ -158,6 +165,8 @@ typedef struct gpumpi_coll_desc {
     uint64_t count;
     void* const* sendbufs;
     void* const* recvbufs;
+    int algo;
+    int pad;
 } gpumpi_coll_desc;
 
 /* Create a communicator of nranks rank blocks with its synchronisation state in HBM. */
@@ -180,6 +189,10 @@ int gpumpi_coll_batched(const gpumpi_coll_desc* descs, int ndesc, int threads_pe
 typedef struct gpumpi_plan_s* gpumpi_plan_t;
 int gpumpi_plan_create(const gpumpi_coll_desc* descs, int ndesc, int threads_per_rank, int batched,
                        gpumpi_plan_t* plan);
+/* As gpumpi_plan_create; plain_threads (may be NULL) gives the threads per
+ * rank of each descriptor's own launch in the plain form. */
+int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, int threads_per_rank, int batched,
+                          const int* plain_threads, gpumpi_plan_t* plan);
 /* Enqueue the plan on a stream (asynchronous). */
 int gpumpi_plan_launch(gpumpi_plan_t plan, void* stream);
 /* Capture the plan's launches once as a CUDA graph; later launches replay it. */
@@ -191,6 +204,24 @@ int gpumpi_plan_capture(gpumpi_plan_t plan, void* stream);
 int gpumpi_plan_run_host(gpumpi_plan_t plan, void* const* host_send, void* const* host_recv,
                          void* stream, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
 int gpumpi_plan_destroy(gpumpi_plan_t plan);
+
+/* Autotuner, on the descriptors' own buffers (their contents are
+ * overwritten).  Plain form: times every candidate schedule (algo) at every
+ * co-resident thread count of each descriptor alone and returns the fastest
+ * in plain_algos[i] and plain_threads[i] (either may be NULL).  Batched form
+ * (when batched_threads is not NULL): measured in the batched launch itself
+ * at every co-resident thread count, then per (collective, type) group; the
+ * choice goes to descs[i].algo and *batched_threads (without it,
+ * descs[i].algo gets the plain choice).  Plain results are cached in
+ * cache_path (one line per shape, thread count and GPU; NULL = no cache).
+ * No counterpart in the reference, whose collectives had one schedule each. */
+typedef struct gpumpi_tune_opts {
+    int reps;                /* timed launches per candidate (0 = 5) */
+    const char* cache_path;
+    int verbose;
+} gpumpi_tune_opts;
+int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_tune_opts* opts, int* batched_threads,
+                    int* plain_threads, int* plain_algos);
 
 /* Error state of the collective API's device job (a timed-out wait, ...);
  * returns GPUMPI_EJOB and clears it when an error was recorded. */
@@ -226,6 +257,9 @@ typedef struct gpumpi_churn_stats {
     double ops_per_s;             /* (allocs + frees) / seconds */
     uint64_t malloc_cycles_p50;   /* malloc latency percentiles in SM cycles */
     uint64_t malloc_cycles_p99;   /*   (lower edge of a quarter-octave bucket) */
+    uint64_t fresh_pages;         /* slab allocator: 64 KiB pages taken from the bump pointer */
+    uint64_t partial_pops;        /*   pages taken from the free-chunk stacks */
+    uint64_t partial_full;        /*   of those, pages that were full again */
 } gpumpi_churn_stats;
 
 /* Every thread of a blocks x threads grid runs `iters` rounds of: malloc of

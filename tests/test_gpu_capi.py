@@ -35,9 +35,12 @@ def _rank_fold(xs, op):
     return acc
 
 
+@pytest.mark.parametrize("algo", [0, 1, 2, 3])
 @pytest.mark.parametrize("form", ["plain", "batched", "graph"])
 @pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (32, 1 << 16)])
-def test_capi_collectives(coll, form, nranks, count):
+def test_capi_collectives(coll, form, nranks, count, algo):
+    """Every schedule (algo 1-3 and the size-based choice 0) folds in rank
+    order, so each gives the host fold's bits."""
     import torch
 
     mod, lib = coll
@@ -72,6 +75,10 @@ def test_capi_collectives(coll, form, nranks, count):
     rd = [torch.zeros(count, dtype=torch.float64, device="cuda") for _ in range(nranks)]
     descs.append(mod.make_desc(comm, mod.COLL_REDUCE, "float64", count, [t.data_ptr() for t in df],
                                [t.data_ptr() for t in rd], mod.OP_PROD, 0, keep))
+    for d in descs:
+        # Reduce has schedules 1 and 2; Allreduce 1-3 (3: every rank pushes its
+        # segment); Alltoall/Allgather 1-3 (3: bulk engine)
+        d.algo = 2 if (d.op == mod.COLL_REDUCE and algo == 3) else algo
     plan = mod.Plan(lib, descs, threads=128, batched=(form != "plain"))
     if form == "graph":
         plan.capture()
@@ -122,6 +129,108 @@ def test_capi_batched_many_comms(coll):
         exp = _rank_fold([x.numpy().astype(np.int32) for x in xs], "sum").astype(np.int32)
         for o in outs:
             assert np.array_equal(o.cpu().numpy(), exp)
+    plan.close()
+    for c in comms:
+        c.close()
+
+
+def test_autotune_picks_valid_schedules_and_keeps_results(coll, tmp_path):
+    """The autotuner times the candidates, caches the plain results, and the
+    tuned plans (plain at per-descriptor schedules and thread counts, batched
+    at its own) give the same bits."""
+
+    import torch
+
+    mod, lib = coll
+    sizes = [4, 24, 128]
+    counts = [1 << 10, 1 << 15, 1 << 18]
+    comms = [mod.Comm(lib, p) for p in sizes]
+    keep, descs, checks = [], [], []
+    g = torch.Generator().manual_seed(11)
+    for c, p, n in zip(comms, sizes, counts):
+        xs = [torch.rand(n, dtype=torch.float64, generator=g) for _ in range(p)]
+        ds = [x.cuda() for x in xs]
+        outs = [torch.empty_like(d) for d in ds]
+        descs.append(mod.make_desc(c, mod.COLL_ALLREDUCE, "float64", n, [d.data_ptr() for d in ds],
+                                   [o.data_ptr() for o in outs], mod.OP_SUM, 0, keep))
+        per = n // p
+        sa = [torch.randint(0, 1 << 30, (per * p,), dtype=torch.int32, generator=g).cuda() for _ in range(p)]
+        ra = [torch.empty_like(t) for t in sa]
+        descs.append(mod.make_desc(c, mod.COLL_ALLTOALL, "int32", per, [t.data_ptr() for t in sa],
+                                   [t.data_ptr() for t in ra], 0, 0, keep))
+        checks.append((xs, ds, outs, sa, ra, per, p))
+    cache = str(tmp_path / "tune.txt")
+    bt, plain, palgos = mod.autotune(lib, descs, reps=3, cache_path=cache)
+    assert bt in (64, 128, 256, 512, 1024)
+    assert all(t in (64, 128, 256, 512, 1024) for t in plain)
+    assert all(d.algo in (1, 2, 3) for d in descs) and all(a in (1, 2, 3) for a in palgos)
+    lines = open(cache).read().splitlines()
+    assert len(descs) <= len(lines) <= 5 * len(descs)
+    # a second run reads the plain results from the cache and returns the same plain choices
+    bt2, plain2, palgos2 = mod.autotune(lib, descs, reps=3, cache_path=cache)
+    assert plain2 == plain and palgos2 == palgos
+    assert len(open(cache).read().splitlines()) == len(lines)
+    pdescs = [type(d).from_buffer_copy(d) for d in descs]
+    for d, a in zip(pdescs, palgos):
+        d.algo = a
+    for batched in (False, True):
+        plan = mod.Plan(lib, descs if batched else pdescs, threads=bt, batched=batched, plain_threads=plain)
+        plan.launch()
+        torch.cuda.synchronize()
+        assert mod.status(lib) is None
+        for xs, ds, outs, sa, ra, per, p in checks:
+            exp = _rank_fold([x.numpy() for x in xs], "sum")
+            for o in outs:
+                assert np.array_equal(o.cpu().numpy().view(np.uint64), exp.view(np.uint64))
+            for r in range(p):
+                got = ra[r].cpu().numpy()
+                for q in range(p):
+                    assert np.array_equal(got[q * per:(q + 1) * per], sa[q].cpu().numpy()[r * per:(r + 1) * per])
+        plan.close()
+    for c in comms:
+        c.close()
+
+
+def test_plan_run_host_with_packed_host_buffers(coll):
+    """Host-buffer entry point: per-rank host and device buffers laid out back
+    to back (copies merge within one allocation) give the same results as the
+    host fold, and the reported byte counts are exact."""
+    import torch
+
+    mod, lib = coll
+    sizes, n = [4, 12, 48], 3000
+    comms = [mod.Comm(lib, p) for p in sizes]
+    keep, descs, layout = [], [], []
+    g = torch.Generator().manual_seed(21)
+    for c, p in zip(comms, sizes):
+        din = torch.empty(p * n, dtype=torch.float64, device="cuda")
+        dout = torch.empty(p * n, dtype=torch.float64, device="cuda")
+        keep.extend([din, dout])
+        descs.append(mod.make_desc(c, mod.COLL_ALLREDUCE, "float64", n, [din.data_ptr() + r * n * 8 for r in range(p)],
+                                   [dout.data_ptr() + r * n * 8 for r in range(p)], mod.OP_SUM, 0, keep))
+        layout.append((p, n * 8))
+    total = sum(p * b for p, b in layout)
+    hs = torch.rand(total // 8, dtype=torch.float64, generator=g).pin_memory()
+    hr = torch.zeros(total // 8, dtype=torch.float64).pin_memory()
+    sp, rp, off = [], [], 0
+    for p, b in layout:
+        for r in range(p):
+            sp.append(hs.data_ptr() + off)
+            rp.append(hr.data_ptr() + off)
+            off += b
+    plan = mod.Plan(lib, descs, threads=128, batched=True)
+    bi, bo = plan.run_host(sp, rp)
+    torch.cuda.synchronize()
+    assert mod.status(lib) is None
+    assert bi == total and bo == total
+    off = 0
+    for p, b in layout:
+        xs = [hs[(off + r * b) // 8:(off + (r + 1) * b) // 8].numpy() for r in range(p)]
+        exp = _rank_fold(xs, "sum")
+        for r in range(p):
+            got = hr[(off + r * b) // 8:(off + (r + 1) * b) // 8].numpy()
+            assert np.array_equal(got.view(np.uint64), exp.view(np.uint64))
+        off += p * b
     plan.close()
     for c in comms:
         c.close()
