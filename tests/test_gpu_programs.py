@@ -111,3 +111,24 @@ def test_gpu_allocator_known_answers(gpu_built, ranks, heap):
     g = gpu_built.run_program("kat_malloc", [], nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=300)
     assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
     assert sorted(g.lines("kat_malloc")) == sorted(f"kat_malloc rank {r} ok" for r in range(ranks))
+
+
+def _cpi_golden():
+    import os
+    rows = []
+    for ln in open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cpi_pi.txt")):
+        if ln.startswith("#") or not ln.strip():
+            continue
+        key, line = ln.rstrip("\n").split(" | ")
+        n, ranks = map(int, key.split())
+        rows.append((n, ranks, line))
+    return rows
+
+
+@pytest.mark.parametrize("n,ranks,line", _cpi_golden())
+def test_gpu_pi_matches_reference_program(gpu_built, n, ranks, line):
+    """GPU run of the converted pi program prints exactly the result line of
+    the reference's cpi.c on a host MPI (committed golden fixture)."""
+    g = gpu_built.run_program("pi", [str(n)], nranks=ranks, extra=GPU_OPTS, timeout=180)
+    assert g.returncode == 0, g.stderr
+    assert g.lines("pi is approximately") == [line]
