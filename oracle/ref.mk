@@ -4,6 +4,10 @@
 # _ref/ (git-ignored).  Needs the reference tree (REF); nothing here runs on
 # the GPU.
 #   make -f ref.mk            cpi and NPB IS classes S, W, A
+#   make -f ref.mk conv       the same programs and global_var.c passed through
+#                             the source converter (_ref/conv/), so a machine
+#                             without the reference tree can build them for the
+#                             GPU and for hostmpi
 REF ?= /root/reference
 NPB := $(REF)/toolchain_tests/npb/NPB3.4.1/NPB3.4-MPI
 O := _ref
@@ -33,4 +37,23 @@ $(O)/is.%: $(NPB)/IS/is.c $(O)/setparams build/libhostmpi.a | $(O)
 	gcc $(CFLAGS) $(NPBDEFS) -I$(O)/is_$* -I$(NPB)/common $< $(NPB)/common/c_print_results.c \
 	    $(NPB)/common/c_timers.c $(LIBS) -o $@
 
-.PHONY: all
+CONV := python3 ../dphpc-project_gb300/gpumpi_convert.py
+C := $(O)/conv
+conv: $(C)/cpi/cpi.cu $(C)/global_var/global_var.cu $(C)/is_S/npbparams.h.cuh \
+      $(C)/is_W/npbparams.h.cuh $(C)/is_A/npbparams.h.cuh
+
+$(C)/cpi/cpi.cu: $(REF)/toolchain_tests/pi/cpi.c ../dphpc-project_gb300/gpumpi_convert.py
+	$(CONV) $< --project $(REF)/toolchain_tests/pi --outdir $(C)/cpi
+
+$(C)/global_var/global_var.cu: $(REF)/toolchain_tests/global_var/global_var.c ../dphpc-project_gb300/gpumpi_convert.py
+	$(CONV) $< --project $(REF)/toolchain_tests/global_var --outdir $(C)/global_var
+
+# npbparams.h per class beside its converted .cuh; the converted IS sources do
+# not depend on the class (it is read from npbparams.h at compile time)
+$(C)/is_%/npbparams.h.cuh: $(NPB)/IS/is.c $(O)/setparams ../dphpc-project_gb300/gpumpi_convert.py
+	mkdir -p $(C)/is_$*
+	cd $(C)/is_$* && ../../setparams is $* > /dev/null 2>&1 ; test -f npbparams.h
+	for f in IS/is.c common/c_print_results.c common/c_timers.c; do \
+	    $(CONV) $(NPB)/$$f --project $(NPB) -I $(C)/is_$* --outdir $(C)/npb || exit 1; done
+
+.PHONY: all conv
