@@ -235,6 +235,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="built-in schedules, --threads for every launch")
     ap.add_argument("--tune-reps", type=int, default=3)
+    ap.add_argument("--profile-launch", action="store_true",
+                    help="bracket one batched launch after the warm-up with cudaProfilerStart/Stop "
+                         "(for ncu --profile-from-start off)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -285,12 +288,18 @@ def main():
         for _ in range(args.warmup):
             plan.launch(stream.cuda_stream)
     torch.cuda.synchronize()
+    if args.profile_launch:
+        torch.cuda.profiler.start()
+        with torch.cuda.stream(stream):
+            plan.launch(stream.cuda_stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         secs = time_plan(torch, plan, args.steps, 0, stream)
-    launches = lib.gpumpi_kernel_launches() - launches0 - args.warmup
+    launches = lib.gpumpi_kernel_launches() - launches0 - args.warmup - int(args.profile_launch)
     err = coll.status(lib)
     if err:
         raise SystemExit(f"device error during benchmark: {err}")
