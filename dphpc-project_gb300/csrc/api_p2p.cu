@@ -11,6 +11,8 @@
 
 using namespace gm;
 
+extern __device__ MPI_Comm_impl gm_world_sentinel;
+
 namespace gm {
 
 __device__ int aborted_code() { return fail_code(bctx().job); }
@@ -67,9 +69,17 @@ static __device__ void empty_status(MPI_Status* st) {
     st->gpumpi_count_hi = 0;
 }
 
+// The abort word is read (relaxed) on every 16th call: an acquire load here
+// would drop the leader's cached rank state from L1 on every call.  Waits read
+// it on every poll, so a rank blocked anywhere still sees an abort at once.
+__device__ __forceinline__ bool api_abort_check(BlockCtx& b) {
+    if ((++b.api_calls & 15u) != 0) return false;
+    return ld_relaxed_int(&b.job->status[0]) != 0;
+}
+
 #define API_ENTER()                                         \
     BlockCtx& b = bctx();                                   \
-    if (job_aborted(b.job)) return aborted_code();
+    if (api_abort_check(b)) return aborted_code();
 
 // ---------------------------------------------------------------- environment
 __device__ int MPI_Init(int* argc, char*** argv) {
@@ -540,8 +550,30 @@ __device__ int MPI_Request_free(MPI_Request* request) {
     return rc;
 }
 
+// A blocking send or receive of at most FAST_MSG_BYTES on MPI_COMM_WORLD, with
+// a basic type, valid arguments and no posted receive or deferred send, takes
+// the leader-only path without a request object.  Anything else (and a full
+// mailbox) goes through the request path, which also reports argument errors.
+static __device__ __forceinline__ bool small_world_call(const BlockCtx& b, MPI_Comm comm, int count,
+                                                        MPI_Datatype datatype, u64* bytes) {
+    if (comm != &gm_world_sentinel || !b.p2p_quiet || count < 0 || (int)datatype < 0 ||
+        (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
+        return false;
+    *bytes = (u64)count * (u64)dtype_size(datatype);
+    return *bytes <= FAST_MSG_BYTES && *bytes <= b.eager_bytes;
+}
+
 __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag,
                         MPI_Comm comm) {
+    {
+        BlockCtx& b = bctx();
+        u64 bytes;
+        if (small_world_call(b, comm, count, datatype, &bytes) && dest >= 0 && dest < b.world_size &&
+            tag >= 0 && tag <= MPI_TAG_UB) {
+            if (api_abort_check(b)) return aborted_code();
+            if (p2p_send_small(buf, bytes, dest, tag)) return MPI_SUCCESS;
+        }
+    }
     MPI_Request r = MPI_REQUEST_NULL;
     int rc = MPI_Isend(buf, count, datatype, dest, tag, comm, &r);
     if (rc) return rc;
@@ -555,6 +587,17 @@ __device__ int MPI_Ssend(const void* buf, int count, MPI_Datatype datatype, int 
 
 __device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source, int tag,
                         MPI_Comm comm, MPI_Status* status) {
+    {
+        BlockCtx& b = bctx();
+        u64 bytes;
+        if (small_world_call(b, comm, count, datatype, &bytes) &&
+            (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
+            (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
+            if (api_abort_check(b)) return aborted_code();
+            int rc = MPI_SUCCESS;
+            if (p2p_recv_small(buf, bytes, source, tag, status, &rc)) return rc;
+        }
+    }
     MPI_Request r = MPI_REQUEST_NULL;
     int rc = start_recv(buf, count, datatype, source, tag, comm, &r, /*try_fast=*/true);
     if (rc) return rc;

@@ -75,7 +75,16 @@ __device__ __noinline__ int dispatch_all(int tid) {
         default: rc = MPI_ERR_INTERN; break;
     }
     bsync();
-    if (tid == 0) c.ret = rc;
+    if (tid == 0) {
+        c.ret = rc;
+        // The lists of posted receives and deferred sends change only in these
+        // calls; the blocking small-message paths run only while both are empty.
+        if (c.op == OP_SEND_START || c.op == OP_RECV_POST || c.op == OP_WAIT || c.op == OP_TEST ||
+            c.op == OP_PROBE || c.op == OP_FINALIZE) {
+            RankPriv* p = b.priv;
+            b.p2p_quiet = p->recv_head < 0 && p->defer_head < 0;
+        }
+    }
     return rc;
 }
 

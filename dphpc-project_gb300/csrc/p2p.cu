@@ -399,12 +399,29 @@ __device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status*
 // are the same as on the block path; anything else (a rendezvous message, a
 // full mailbox) falls back to the block path before touching any state.
 
+// One thread copies 16-byte vectors, 8 loads in flight before their stores (a
+// load-store-load chain would wait a memory round trip per vector, as the
+// compiler cannot move a load above a store that may alias it).  `cg`: the
+// source is read through L2 (data another SM wrote).
+template <bool cg>
+static __device__ __forceinline__ void copy_vec16(uint4* d, const uint4* s, u64 nv) {
+    u64 i = 0;
+    for (; i + 8 <= nv; i += 8) {
+        uint4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = cg ? __ldcg(s + i + k) : s[i + k];
+#pragma unroll
+        for (int k = 0; k < 8; k++) d[i + k] = v[k];
+    }
+    for (; i < nv; i++) d[i] = cg ? __ldcg(s + i) : s[i];
+}
+
 static __device__ void leader_copy(void* dst, const void* src, u64 n) {
     char* d = (char*)dst;
     const char* s = (const char*)src;
     if ((((uintptr_t)d | (uintptr_t)s) & 15) == 0) {
         const u64 nv = n >> 4;
-        for (u64 i = 0; i < nv; i++) ((uint4*)d)[i] = ((const uint4*)s)[i];
+        copy_vec16<false>((uint4*)d, (const uint4*)s, nv);
         for (u64 i = nv << 4; i < n; i++) d[i] = s[i];
     } else if ((((uintptr_t)d | (uintptr_t)s) & 7) == 0) {
         const u64 nv = n >> 3;
@@ -427,6 +444,137 @@ __device__ bool p2p_send_fast(MPI_Request_impl* r) {
     red_or_release(&j->mbox[r->peer_world].ready, 1ull << slot);
     r->state = RS_DONE;
     return true;
+}
+
+// Leader: blocking send of a small eager message on MPI_COMM_WORLD, without a
+// request object.  Reads only the block's shared-memory copies of job state;
+// the stamp and the slot claim are in flight together.  Returns 0 (before
+// publishing anything) when the destination's mailbox is full.
+__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag) {
+    BlockCtx& b = bctx();
+    Mailbox* mb = &b.mbox[dest];
+    const u64 stamp = atomicAdd(&mb->stamp, 1ull);   // a skipped stamp only leaves a gap
+    // up to 64 aligned bytes are loaded now, while the atomics are in flight
+    const bool pre = bytes <= 64 && ((uintptr_t)buf & 15) == 0;
+    uint4 v[4];
+    if (pre) {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if ((u64)k * 16 < bytes) v[k] = ((const uint4*)buf)[k];
+    }
+    u64 used = b.slot_hint;
+    int s;
+    for (int tries = 0;; tries++) {
+        if (~used == 0) {
+            if (tries) return 0;
+            used = ld_relaxed(&mb->used);
+            if (~used == 0) return 0;
+        }
+        s = __ffsll((long long)~used) - 1;
+        const u64 bit = 1ull << s;
+        // acquire: the slot is written only after the receiver released it
+        const u64 old = atom_or_acquire(&mb->used, bit);
+        if (!(old & bit)) {
+            b.slot_hint = old | bit;
+            break;
+        }
+        used = old | bit;
+    }
+    MsgHdr* h = &mb->hdr[s];
+    *(int4*)h = make_int4(b.world_ctx, b.rank, tag, 0);   // ctx, src, tag, kind = eager
+    *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
+    char* slot = b.eager + ((u64)dest * MB_SLOTS + s) * b.eager_bytes;
+    if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if ((u64)k * 16 < bytes) ((uint4*)slot)[k] = v[k];
+    } else if (bytes) {
+        leader_copy(slot, buf, bytes);
+    }
+    red_or_release(&mb->ready, 1ull << s);
+    return 1;
+}
+
+// Leader: blocking receive of a small eager message on MPI_COMM_WORLD without
+// a request object.  The header's first 32 bytes are read as two vectors and,
+// for messages of up to 16 bytes, the payload with them.
+__device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    Mailbox* mb = &b.mbox[b.rank];
+    const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
+    const u64 t0 = gtime();
+    unsigned ns = 32;
+    for (;;) {
+        // acquire on every poll: nothing read after it comes from L1 anyway
+        u64 ready = ld_acquire(&mb->ready);
+        if (ready) {
+            int best = -1;
+            u64 best_stamp = ~0ull, best_bytes = 0;
+            int best_src = 0, best_tag = 0, best_kind = 0;
+            uint4 pre = make_uint4(0, 0, 0, 0);
+            while (ready) {
+                const int s = __ffsll((long long)ready) - 1;
+                ready &= ready - 1;
+                const int4 h0 = __ldcg((const int4*)&mb->hdr[s]);
+                const ulonglong2 h1 = __ldcg((const ulonglong2*)&mb->hdr[s].bytes);
+                const uint4 p0 = __ldcg((const uint4*)(slots + (u64)s * b.eager_bytes));
+                if (h0.x != b.world_ctx) continue;
+                if (source != MPI_ANY_SOURCE && h0.y != source) continue;
+                if (tag != MPI_ANY_TAG && h0.z != tag) continue;
+                if (h1.y < best_stamp) {
+                    best_stamp = h1.y;
+                    best = s;
+                    best_src = h0.y;
+                    best_tag = h0.z;
+                    best_kind = h0.w;
+                    best_bytes = h1.x;
+                    pre = p0;
+                }
+            }
+            if (best >= 0) {
+                if (best_kind != 0 || best_bytes > FAST_MSG_BYTES) return 0;   // request path
+                const u64 n = best_bytes < bytes ? best_bytes : bytes;
+                char* d = (char*)buf;
+                if (n <= 16) {
+                    const char* pc = (const char*)&pre;
+                    for (u64 i = 0; i < n; i++) d[i] = pc[i];
+                } else {
+                    const char* src = slots + (u64)best * b.eager_bytes;
+                    u64 i = 0;
+                    if (((uintptr_t)d & 15) == 0) {
+                        copy_vec16<true>((uint4*)d, (const uint4*)src, n >> 4);
+                        i = n & ~(u64)15;
+                    } else if (((uintptr_t)d & 7) == 0) {
+                        for (; i + 8 <= n; i += 8) *(u64*)(d + i) = __ldcg((const u64*)(src + i));
+                    }
+                    for (; i < n; i++) d[i] = __ldcg(src + i);
+                }
+                red_and_relaxed(&mb->ready, ~(1ull << best));
+                red_and_release(&mb->used, ~(1ull << best));
+                *rc = best_bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
+                if (st) {
+                    st->MPI_SOURCE = best_src;
+                    st->MPI_TAG = best_tag;
+                    st->MPI_ERROR = *rc;
+                    st->gpumpi_count_lo = (int)(n & 0xffffffffu);
+                    st->gpumpi_count_hi = (int)(n >> 32);
+                }
+                return 1;
+            }
+        }
+        if (ld_relaxed_int(&j->status[0]) != 0) {
+            *rc = fail_code(j);
+            return 1;
+        }
+        if (gtime() - t0 > b.timeout_ns) {
+            job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
+            *rc = GPUMPI_ERR_TIMEOUT;
+            return 1;
+        }
+        __nanosleep(ns);
+        if (ns < 128) ns <<= 1;
+    }
 }
 
 // Leader: blocking receive of a small eager message into r (r->buf may be

@@ -328,6 +328,11 @@ __device__ __forceinline__ int ld_acquire_int(const int* p) {
     asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ int ld_relaxed_int(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_release(u64* p, u64 v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -463,6 +468,17 @@ struct BlockCtx {
     int in_call;                  // leader is inside block_call (helpers busy)
     int bulk_broken;              // a bulk pipeline failed with loads possibly in flight:
                                   // its barriers may not be initialised again
+    // The leader's copies of what the blocking small-message paths read, so
+    // that they touch no rank-private global state: a gpu-scope acquire drops
+    // the SM's L1, after which every such read would be an L2 round trip.
+    Mailbox* mbox;                // job's mailboxes (indexed by world rank)
+    char* eager;                  // job's eager slots
+    u64 eager_bytes;
+    u64 timeout_ns;
+    u64 slot_hint;                // `used` bits last seen at a destination
+    int world_ctx, world_size;
+    int p2p_quiet;                // no posted receive and no deferred send
+    unsigned api_calls;           // counts calls between checks of the abort word
 };
 
 static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");
@@ -572,6 +588,11 @@ __device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, i
 // p2p engine (block-cooperative)
 __device__ int p2p_send_start(MPI_Request_impl* r, int tid, int T);
 constexpr u64 FAST_MSG_BYTES = 1024;   // eager messages the leader moves alone
+// Blocking send/receive of a small eager message on MPI_COMM_WORLD by the
+// leader, without a request object.  Return 1 when done (*rc set), 0 when the
+// request path must take the call.
+__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag);
+__device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc);
 __device__ bool p2p_send_fast(MPI_Request_impl* r);
 __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled);
 __device__ int p2p_recv_post(MPI_Request_impl* r, int tid, int T);

@@ -388,6 +388,15 @@ __device__ void rank_init(int tid, int T) {
         w.kind = 1;
         w.ctx = 1;
         w.size = j->nranks;
+        b.mbox = j->mbox;
+        b.eager = j->eager;
+        b.eager_bytes = j->eager_bytes;
+        b.timeout_ns = j->timeout_ns;
+        b.slot_hint = 0;
+        b.world_ctx = 1;
+        b.world_size = j->nranks;
+        b.p2p_quiet = 1;
+        b.api_calls = 0;
         w.rank = r;
         w.refcnt = 1;
         w.cs = j->world_cs;
