@@ -550,17 +550,18 @@ __device__ int MPI_Request_free(MPI_Request* request) {
     return rc;
 }
 
-// A blocking send or receive of at most FAST_MSG_BYTES on MPI_COMM_WORLD, with
-// a basic type, valid arguments and no posted receive or deferred send, takes
-// the leader-only path without a request object.  Anything else (and a full
-// mailbox) goes through the request path, which also reports argument errors.
+// A blocking send or receive of an eager message on MPI_COMM_WORLD, with a
+// basic type, valid arguments and no posted receive or deferred send, takes
+// the leader-only path without a request object (p2p_send_small and
+// p2p_recv_small decide by size and buffer).  Anything else, and a full
+// mailbox, goes through the request path, which also reports argument errors.
 static __device__ __forceinline__ bool small_world_call(const BlockCtx& b, MPI_Comm comm, int count,
                                                         MPI_Datatype datatype, u64* bytes) {
     if (comm != &gm_world_sentinel || !b.p2p_quiet || count < 0 || (int)datatype < 0 ||
         (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
         return false;
     *bytes = (u64)count * (u64)dtype_size(datatype);
-    return *bytes <= FAST_MSG_BYTES && *bytes <= b.eager_bytes;
+    return true;
 }
 
 __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag,
@@ -568,10 +569,11 @@ __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int d
     {
         BlockCtx& b = bctx();
         u64 bytes;
-        if (small_world_call(b, comm, count, datatype, &bytes) && dest >= 0 && dest < b.world_size &&
-            tag >= 0 && tag <= MPI_TAG_UB) {
+        if (small_world_call(b, comm, count, datatype, &bytes) && bytes <= b.eager_bytes && dest >= 0 &&
+            dest < b.world_size && tag >= 0 && tag <= MPI_TAG_UB) {
             if (api_abort_check(b)) return aborted_code();
-            if (p2p_send_small(buf, bytes, dest, tag)) return MPI_SUCCESS;
+            int rc = MPI_SUCCESS;
+            if (p2p_send_small(buf, bytes, dest, tag, &rc)) return rc;
         }
     }
     MPI_Request r = MPI_REQUEST_NULL;

@@ -450,8 +450,25 @@ __device__ bool p2p_send_fast(MPI_Request_impl* r) {
 // request object.  Reads only the block's shared-memory copies of job state;
 // the stamp and the slot claim are in flight together.  Returns 0 (before
 // publishing anything) when the destination's mailbox is full.
-__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag) {
+// The leader alone copies n bytes (a multiple of 16) between 16-byte aligned
+// global buffers through the bulk engine: one load and one store round trip,
+// whatever n.  Returns 0 or an error code (the job has then failed).
+static __device__ int leader_bulk_copy(char* dst, const char* src, u64 n) {
+    BulkPipe bp;
+    if (!bp.begin()) return MPI_ERR_INTERN;   // not reached: leader_bulk_ok checked the area
+    bp.push(dst, src, n);
+    return bp.finish();
+}
+
+static __device__ __forceinline__ bool leader_bulk_ok(const void* p, u64 n) {
+    return n >= SMALL_BULK_MIN && ((uintptr_t)p & 15) == 0 && is_global(p) && !bctx().bulk_broken &&
+           bulk_stage_bytes() >= 8192;
+}
+
+__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc) {
     BlockCtx& b = bctx();
+    const bool bulk = leader_bulk_ok(buf, bytes);
+    if (bytes > FAST_MSG_BYTES && !bulk) return 0;
     Mailbox* mb = &b.mbox[dest];
     const u64 stamp = atomicAdd(&mb->stamp, 1ull);   // a skipped stamp only leaves a gap
     // up to 64 aligned bytes are loaded now, while the atomics are in flight
@@ -484,10 +501,16 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag) {
     *(int4*)h = make_int4(b.world_ctx, b.rank, tag, 0);   // ctx, src, tag, kind = eager
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
     char* slot = b.eager + ((u64)dest * MB_SLOTS + s) * b.eager_bytes;
+    *rc = MPI_SUCCESS;
     if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
 #pragma unroll
         for (int k = 0; k < 4; k++)
             if ((u64)k * 16 < bytes) ((uint4*)slot)[k] = v[k];
+    } else if (bulk) {
+        const u64 n16 = bytes & ~(u64)15;
+        *rc = leader_bulk_copy(slot, (const char*)buf, n16);
+        if (*rc) return 1;   // the job has failed; nothing is published
+        for (u64 i = n16; i < bytes; i++) slot[i] = ((const char*)buf)[i];
     } else if (bytes) {
         leader_copy(slot, buf, bytes);
     }
@@ -533,10 +556,18 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
                 }
             }
             if (best >= 0) {
-                if (best_kind != 0 || best_bytes > FAST_MSG_BYTES) return 0;   // request path
+                if (best_kind != 0) return 0;   // rendezvous: request path
                 const u64 n = best_bytes < bytes ? best_bytes : bytes;
+                const bool bulk = leader_bulk_ok(buf, n);
+                if (n > FAST_MSG_BYTES && !bulk) return 0;
                 char* d = (char*)buf;
-                if (n <= 16) {
+                if (bulk) {
+                    const u64 n16 = n & ~(u64)15;
+                    const char* src = slots + (u64)best * b.eager_bytes;
+                    *rc = leader_bulk_copy(d, src, n16);
+                    if (*rc) return 1;   // the job has failed; the slot stays claimed
+                    for (u64 i = n16; i < n; i++) d[i] = __ldcg(src + i);
+                } else if (n <= 16) {
                     const char* pc = (const char*)&pre;
                     for (u64 i = 0; i < n; i++) d[i] = pc[i];
                 } else {

@@ -588,10 +588,13 @@ __device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, i
 // p2p engine (block-cooperative)
 __device__ int p2p_send_start(MPI_Request_impl* r, int tid, int T);
 constexpr u64 FAST_MSG_BYTES = 1024;   // eager messages the leader moves alone
-// Blocking send/receive of a small eager message on MPI_COMM_WORLD by the
-// leader, without a request object.  Return 1 when done (*rc set), 0 when the
-// request path must take the call.
-__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag);
+constexpr u64 SMALL_BULK_MIN = 512;    // leader copies from this size go through the bulk engine
+// Blocking send/receive of an eager message on MPI_COMM_WORLD by the leader,
+// without a request object: up to FAST_MSG_BYTES always, up to the eager size
+// when the user buffer is global, 16-byte aligned and the block has a bulk
+// staging area.  Return 1 when done (*rc set), 0 when the request path must
+// take the call.
+__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
 __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc);
 __device__ bool p2p_send_fast(MPI_Request_impl* r);
 __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled);

@@ -1138,6 +1138,17 @@ class Unit:
         if b == a + 1 and self.kind(a) == "id":
             v = self._lookup(scopes, self.t(a))
             return v is not None and v.ctype is not None and v.ctype.replace(" ", "") == "void*"
+        if b - a >= 3 and self.t(b - 2) in ("->", ".") and self.kind(b - 1) == "id":
+            # a member access chain (`p->next->data`, `s.buf`) ending in a `void *` member
+            q = a
+            while q < b - 2:
+                if self.t(q) in ("(", "["):
+                    q = self.match[q] + 1
+                elif self.kind(q) == "id" or self.t(q) in ("->", "."):
+                    q += 1
+                else:
+                    return False
+            return (self.syms.members.get(self.t(b - 1)) or "").replace(" ", "") == "void*"
         return False
 
     # ---- post-pass: coalescing arguments and empty prototypes

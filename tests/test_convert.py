@@ -4,8 +4,8 @@ Rules: each rewrite of source_converter/converter.cpp checked on a small
 input.  Semantics: the converter's test programs (tests/convert_cases/*.c)
 run unmodified and converted on the hostmpi oracle and print the same lines;
 their converted forms compile for sm_103a.  Reference programs (when the
-reference tree is present): cpi.c, global_var.c and NPB IS pass through the
-converter and still give the reference's answers on the oracle.
+reference tree is present): cpi.c, global_var.c, NPB IS and NPB DT pass
+through the converter and still give the reference's answers on the oracle.
 """
 import os
 import subprocess
@@ -151,6 +151,10 @@ void f(void) {
     assert "__gpu_global(g) = (int *)raw;" in out
     assert "rows[0] = (int *)malloc(4);" in out
     assert "use((int *)malloc(4));" in out
+    # a `void *` struct member read into a typed pointer, and returned as one
+    out = C(conv, "typedef struct { void *head; } Q;\nint *first(Q *q) { int *h;\n h = q->head;\n return q->head; }\n")
+    assert "h = (int *)q->head;" in out
+    assert "return (int *)q->head;" in out
 
 
 def test_cxx_keywords_restrict_includes_and_dead_code(conv):
@@ -313,6 +317,22 @@ def test_converted_reference_global_var_passes(ref_conv, tmp_path):
     exe = _host_build([os.path.join(ref_conv, "conv", "global_var", "global_var.cu")], str(tmp_path / "gv"))
     r = subprocess.run([exe, "---gpumpi", "-n", "4"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "error" not in r.stdout
+
+
+@pytest.mark.parametrize("graph,ranks", [("BH", 5), ("WH", 8), ("SH", 12)])
+def test_converted_reference_npb_dt_matches_the_unmodified_build(ref_conv, tmp_path, graph, ranks):
+    npb = os.path.join(ref_conv, "conv", "npb")
+    exe = _host_build([os.path.join(npb, "DT", "dt.cu"), os.path.join(npb, "DT", "DGraph.cu"),
+                       os.path.join(npb, "common", "randdp.cu"), os.path.join(npb, "common", "c_print_results.cu"),
+                       os.path.join(npb, "common", "c_timers.cu")], str(tmp_path / "dt"),
+                      ["-I" + os.path.join(ref_conv, "conv", "dt_S")] + NPBDEFS)
+    run = lambda e: subprocess.run([e, graph, "---gpumpi", "-n", str(ranks)], capture_output=True, text=True,
+                                   timeout=300)  # noqa: E731
+    got, want = run(exe), run(os.path.join(ref_conv, "dt.S"))
+    assert got.returncode == 0 and want.returncode == 0
+    assert "Verification    =               SUCCESSFUL" in got.stdout
+    strip = lambda s: [x for x in s.splitlines() if not _unstable(x)]  # noqa: E731
+    assert strip(got.stdout) == strip(want.stdout)
 
 
 @pytest.mark.parametrize("cls,ranks", [("S", 2), ("W", 4)])

@@ -5,8 +5,9 @@ compiled on this machine, run by the device runtime, and must print what the
 unmodified C program prints on the hostmpi oracle.  When the converted forms
 of the reference's own programs are present (oracle/_ref/conv, made from the
 reference tree by `make -C oracle -f ref.mk conv`), those run too: cpi.c must
-print the golden lines, global_var.c must report no error, and NPB IS must pass
-its own verification and print what the oracle build of the same source prints.
+print the golden lines, global_var.c must report no error, and NPB IS and DT
+must pass their own verification and print what the oracle build of the same
+source prints.
 """
 import os
 import subprocess
@@ -124,5 +125,33 @@ def test_gpu_converted_npb_is_verifies_and_matches_hostmpi(npb_is, cls, ranks):
     gpu, host = npb_is[cls]
     got = _run([gpu, "---gpumpi", "-n", str(ranks), "-p", "4G", *GPU_OPTS], timeout=400)
     want = _run([host, "---gpumpi", "-n", str(ranks)], timeout=400)
+    assert "Verification    =               SUCCESSFUL" in got
+    assert _stable(got) == _stable(want)
+
+
+@pytest.fixture(scope="module")
+def npb_dt(gpu_built, tmp_path_factory):
+    if not os.path.isdir(os.path.join(CONV, "dt_S")):
+        pytest.skip("converted reference programs absent")
+    d = tmp_path_factory.mktemp("npb_dt")
+    npb = os.path.join(CONV, "npb")
+    srcs = [os.path.join(npb, "DT", "dt.cu"), os.path.join(npb, "DT", "DGraph.cu"),
+            os.path.join(npb, "common", "randdp.cu"), os.path.join(npb, "common", "c_print_results.cu"),
+            os.path.join(npb, "common", "c_timers.cu")]
+    inc = "-I" + os.path.join(CONV, "dt_S")
+    gpu = str(d / "dt_gpu.S")
+    _gpumpicc([*srcs, inc, *NPBDEFS, "-o", gpu], cwd=str(d))
+    host = str(d / "dt_host.S")
+    _check(subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-w", "-x", "c++", "-I" + HOSTINC, inc,
+                           *NPBDEFS, *srcs, "-x", "none", HOSTLIB, "-lpthread", "-o", host],
+                          capture_output=True, text=True))
+    return gpu, host
+
+
+@pytest.mark.parametrize("graph,ranks", [("BH", 5), ("WH", 8), ("SH", 12), ("SH", 21)])
+def test_gpu_converted_npb_dt_verifies_and_matches_hostmpi(npb_dt, graph, ranks):
+    gpu, host = npb_dt
+    got = _run([gpu, graph, "---gpumpi", "-n", str(ranks), *GPU_OPTS], timeout=400)
+    want = _run([host, graph, "---gpumpi", "-n", str(ranks)], timeout=400)
     assert "Verification    =               SUCCESSFUL" in got
     assert _stable(got) == _stable(want)

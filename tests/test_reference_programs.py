@@ -4,7 +4,9 @@ oracle/ref.mk compiles, by path, the reference's pi example
 (toolchain_tests/pi/cpi.c) and the vendored NPB IS kernel
 (toolchain_tests/npb/NPB3.4.1/NPB3.4-MPI/IS/is.c, classes S, W and A, whose
 built-in full verification checks the ranks against the class's known
-answers, is.c:261-296 and 561-629) against hostmpi.  Skipped when the
+answers, is.c:261-296 and 561-629) and NPB DT class S (DT/dt.c, verified
+against its known L2 norms, dt.c:78-170, on the BH, WH and SH graphs)
+against hostmpi.  Skipped when the
 reference tree is not present.
 """
 import os
@@ -29,6 +31,14 @@ def ref_built(oracle_built):
 @pytest.mark.parametrize("cls,ranks", [("S", 1), ("S", 2), ("S", 4), ("W", 4), ("W", 8), ("A", 4)])
 def test_npb_is_verifies_on_the_oracle(ref_built, cls, ranks):
     r = subprocess.run([os.path.join(ref_built, f"is.{cls}"), "---gpumpi", "-n", str(ranks)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Verification    =               SUCCESSFUL" in r.stdout
+
+
+@pytest.mark.parametrize("graph,ranks", [("BH", 5), ("WH", 8), ("SH", 12)])
+def test_npb_dt_verifies_on_the_oracle(ref_built, graph, ranks):
+    r = subprocess.run([os.path.join(ref_built, "dt.S"), graph, "---gpumpi", "-n", str(ranks)],
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "Verification    =               SUCCESSFUL" in r.stdout
