@@ -301,7 +301,9 @@ size_t pick_rank_smem(const void* kernel, int T, int need) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const size_t stages[] = {65536, 32768, 16384, 8192};
+    // the largest staging area that keeps every rank block resident (a bulk
+    // copy has stage bytes in flight per block)
+    const size_t stages[] = {65536, 49152, 40960, 32768, 28672, 24576, 20480, 16384, 12288, 8192};
     for (size_t st : stages) {
         const size_t smem = rank_smem_bytes(st);
         if (smem > 48 * 1024 &&

@@ -205,12 +205,22 @@ __device__ bool BulkPipe::retire() {
     return true;
 }
 
+// Schedule: at most BULK_STAGES - 1 loads wait; before a load reuses a stage,
+// the oldest load is retired (its store issued) and only the store issued one
+// step earlier, which used this stage, must have finished reading it; the
+// newest store may still be reading its own stage.
 __device__ bool BulkPipe::push(char* dst, const char* src, u64 n) {
     while (n > 0 && !err) {
         const u32 len = n < chunk ? (u32)n : chunk;
-        if (issued - stored == BULK_STAGES && !retire()) return false;
-        // the stage is free once the store that last used it has read it
-        if (issued >= BULK_STAGES) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        if (issued - stored == BULK_STAGES - 1 && !retire()) return false;
+        // the stage is free once the store that last used it (#issued - BULK_STAGES) has read it;
+        // stores newer than that one may stay in flight
+        if (issued >= BULK_STAGES) {
+            if (stored - (issued - BULK_STAGES) >= 2)
+                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+            else
+                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
         const int s = (int)(issued % BULK_STAGES);
         const u32 bar = smem_u32(&bars[s]);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(len) : "memory");
