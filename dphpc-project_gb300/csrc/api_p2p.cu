@@ -569,11 +569,13 @@ __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int d
     {
         BlockCtx& b = bctx();
         u64 bytes;
-        if (small_world_call(b, comm, count, datatype, &bytes) && bytes <= b.eager_bytes && dest >= 0 &&
-            dest < b.world_size && tag >= 0 && tag <= MPI_TAG_UB) {
+        if (small_world_call(b, comm, count, datatype, &bytes) && dest >= 0 && dest < b.world_size &&
+            tag >= 0 && tag <= MPI_TAG_UB) {
             if (api_abort_check(b)) return aborted_code();
             int rc = MPI_SUCCESS;
-            if (p2p_send_small(buf, bytes, dest, tag, &rc)) return rc;
+            if (bytes <= b.eager_bytes ? p2p_send_small(buf, bytes, dest, tag, &rc)
+                                       : p2p_send_rdv_small(buf, bytes, dest, tag, &rc))
+                return rc;
         }
     }
     MPI_Request r = MPI_REQUEST_NULL;

@@ -465,6 +465,68 @@ static __device__ __forceinline__ bool leader_bulk_ok(const void* p, u64 n) {
            bulk_stage_bytes() >= 8192;
 }
 
+// Leader: claim a free slot of mailbox mb (first guess from the bits last seen
+// there), or -1 when it is full.
+static __device__ int claim_slot_small(Mailbox* mb) {
+    BlockCtx& b = bctx();
+    u64 used = b.slot_hint;
+    for (int tries = 0;; tries++) {
+        if (~used == 0) {
+            if (tries) return -1;
+            used = ld_relaxed(&mb->used);
+            if (~used == 0) return -1;
+        }
+        const int s = __ffsll((long long)~used) - 1;
+        const u64 bit = 1ull << s;
+        // acquire: the slot is written only after the receiver released it
+        const u64 old = atom_or_acquire(&mb->used, bit);
+        if (!(old & bit)) {
+            b.slot_hint = old | bit;
+            return s;
+        }
+        used = old | bit;
+    }
+}
+
+// Leader: blocking rendezvous send on MPI_COMM_WORLD without a request object.
+// The header points the receiver at the user's (global) buffer and at the
+// rank's completion word; the call returns once the receiver has copied the
+// data and set that word.  Returns 0 (before publishing) when buf is not in
+// global memory or the mailbox is full.
+__device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest, int tag, int* rc) {
+    BlockCtx& b = bctx();
+    if (!is_global(buf)) return 0;
+    Mailbox* mb = &b.mbox[dest];
+    const u64 stamp = atomicAdd(&mb->stamp, 1ull);
+    u32* done = &b.priv->rdv_done_small;
+    *done = 0u;
+    const int s = claim_slot_small(mb);
+    if (s < 0) return 0;
+    MsgHdr* h = &mb->hdr[s];
+    *(int4*)h = make_int4(b.world_ctx, b.rank, tag, 1);   // kind = rendezvous
+    *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
+    *(ulonglong2*)&h->rdv_src = make_ulonglong2((u64)buf, (u64)done);
+    red_or_release(&mb->ready, 1ull << s);
+    Job* j = b.job;
+    const u64 t0 = gtime();
+    unsigned ns = 32;
+    while (!ld_acquire32(done)) {
+        if (ld_relaxed_int(&j->status[0]) != 0) {
+            *rc = fail_code(j);
+            return 1;
+        }
+        if (gtime() - t0 > b.timeout_ns) {
+            job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
+            *rc = GPUMPI_ERR_TIMEOUT;
+            return 1;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+    }
+    *rc = MPI_SUCCESS;
+    return 1;
+}
+
 __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc) {
     BlockCtx& b = bctx();
     const bool bulk = leader_bulk_ok(buf, bytes);
@@ -479,24 +541,8 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int
         for (int k = 0; k < 4; k++)
             if ((u64)k * 16 < bytes) v[k] = ((const uint4*)buf)[k];
     }
-    u64 used = b.slot_hint;
-    int s;
-    for (int tries = 0;; tries++) {
-        if (~used == 0) {
-            if (tries) return 0;
-            used = ld_relaxed(&mb->used);
-            if (~used == 0) return 0;
-        }
-        s = __ffsll((long long)~used) - 1;
-        const u64 bit = 1ull << s;
-        // acquire: the slot is written only after the receiver released it
-        const u64 old = atom_or_acquire(&mb->used, bit);
-        if (!(old & bit)) {
-            b.slot_hint = old | bit;
-            break;
-        }
-        used = old | bit;
-    }
+    const int s = claim_slot_small(mb);
+    if (s < 0) return 0;
     MsgHdr* h = &mb->hdr[s];
     *(int4*)h = make_int4(b.world_ctx, b.rank, tag, 0);   // ctx, src, tag, kind = eager
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
@@ -556,14 +602,23 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
                 }
             }
             if (best >= 0) {
-                if (best_kind != 0) return 0;   // rendezvous: request path
                 const u64 n = best_bytes < bytes ? best_bytes : bytes;
                 const bool bulk = leader_bulk_ok(buf, n);
-                if (n > FAST_MSG_BYTES && !bulk) return 0;
+                u32* rdv_done = nullptr;
+                const char* rdv_src = nullptr;
+                if (best_kind != 0) {
+                    // rendezvous: the leader pulls from the sender's buffer when the bulk engine applies
+                    const ulonglong2 h2 = __ldcg((const ulonglong2*)&mb->hdr[best].rdv_src);
+                    rdv_src = (const char*)h2.x;
+                    rdv_done = (u32*)h2.y;
+                    if (!bulk || ((uintptr_t)rdv_src & 15) != 0) return 0;   // request path
+                } else if (n > FAST_MSG_BYTES && !bulk) {
+                    return 0;
+                }
                 char* d = (char*)buf;
                 if (bulk) {
                     const u64 n16 = n & ~(u64)15;
-                    const char* src = slots + (u64)best * b.eager_bytes;
+                    const char* src = rdv_src ? rdv_src : slots + (u64)best * b.eager_bytes;
                     *rc = leader_bulk_copy(d, src, n16);
                     if (*rc) return 1;   // the job has failed; the slot stays claimed
                     for (u64 i = n16; i < n; i++) d[i] = __ldcg(src + i);
@@ -582,6 +637,10 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
                     for (; i < n; i++) d[i] = __ldcg(src + i);
                 }
                 red_and_relaxed(&mb->ready, ~(1ull << best));
+                if (rdv_done) {
+                    __threadfence();
+                    st_release32(rdv_done, 1u);
+                }
                 red_and_release(&mb->used, ~(1ull << best));
                 *rc = best_bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
                 if (st) {

@@ -198,6 +198,7 @@ struct Heap;
 
 // Per-rank state touched only by the rank's own block.
 struct RankPriv {
+    u32 rdv_done_small;            // completion word of the leader's blocking rendezvous send
     MPI_Request_impl* reqs;
     int nreqs;
     int free_head;
@@ -595,6 +596,7 @@ constexpr u64 SMALL_BULK_MIN = 512;    // leader copies from this size go throug
 // staging area.  Return 1 when done (*rc set), 0 when the request path must
 // take the call.
 __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
+__device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
 __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc);
 __device__ bool p2p_send_fast(MPI_Request_impl* r);
 __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled);
