@@ -10,10 +10,15 @@
 #include <time.h>
 
 #include <string>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "gpumpi.h"
 #include "hostjob.h"
+
+#include <map>
+#include <mutex>
 #include "rt.cuh"
 
 static_assert(GPUMPI_DT_INT == MPI_INT && GPUMPI_DT_DOUBLE == MPI_DOUBLE && GPUMPI_DT_BYTE == MPI_BYTE &&
@@ -295,6 +300,24 @@ static double now_s() {
     return ts.tv_sec + ts.tv_nsec * 1e-9;
 }
 
+// A kernel's cudaFuncAttributeMaxDynamicSharedMemorySize is the most dynamic
+// shared memory any of its launches may use.  It only ever grows here: a size
+// picked for one launch must stay allowed after a later pick for another
+// launch of the same kernel tried (and set) other sizes.
+static bool allow_dynamic_smem(const void* kernel, size_t smem) {
+    static std::mutex mu;
+    static std::map<const void*, size_t> allowed;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = allowed[kernel];
+    if (smem <= 48 * 1024 || smem <= cur) return true;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cur = smem;
+    return true;
+}
+
 // Choose threads per rank: the largest of 256/128/64 that keeps every rank
 // resident, given the kernel's register and shared-memory use.
 size_t pick_rank_smem(const void* kernel, int T, int need) {
@@ -303,14 +326,11 @@ size_t pick_rank_smem(const void* kernel, int T, int need) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     // the largest staging area that keeps every rank block resident (a bulk
     // copy has stage bytes in flight per block)
-    const size_t stages[] = {65536, 49152, 40960, 32768, 28672, 24576, 20480, 16384, 12288, 8192};
+    const size_t stages[] = {196608, 131072, 98304, 65536, 49152, 40960, 32768, 28672, 24576, 20480,
+                             16384, 12288, 8192};
     for (size_t st : stages) {
         const size_t smem = rank_smem_bytes(st);
-        if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
+        if (!allow_dynamic_smem(kernel, smem)) continue;
         int per = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem) != cudaSuccess) {
             cudaGetLastError();

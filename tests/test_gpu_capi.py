@@ -191,6 +191,38 @@ def test_autotune_picks_valid_schedules_and_keeps_results(coll, tmp_path):
         c.close()
 
 
+def test_plain_plan_launches_with_different_staging_sizes(coll):
+    """Plain launches of one plan get different staging areas (a 4-rank launch
+    the largest, a 256-rank launch a smaller one); every launch must still be
+    allowed its own size after the later picks, and give the rank-order fold."""
+    import torch
+
+    mod, lib = coll
+    keep, descs, checks, comms = [], [], [], []
+    g = torch.Generator().manual_seed(5)
+    for p, n in ((4, 1 << 16), (4, 1 << 14), (256, 1 << 12)):
+        c = mod.Comm(lib, p)
+        comms.append(c)
+        xs = [torch.rand(n, dtype=torch.float64, generator=g) for _ in range(p)]
+        ds = [x.cuda() for x in xs]
+        outs = [torch.empty_like(d) for d in ds]
+        descs.append(mod.make_desc(c, mod.COLL_ALLREDUCE, "float64", n, [d.data_ptr() for d in ds],
+                                   [o.data_ptr() for o in outs], mod.OP_SUM, 0, keep))
+        checks.append((xs, ds, outs))
+    plan = mod.Plan(lib, descs, threads=128, batched=False)
+    for _ in range(2):
+        plan.launch()
+        torch.cuda.synchronize()
+        assert mod.status(lib) is None
+    for xs, ds, outs in checks:
+        exp = _rank_fold([x.numpy() for x in xs], "sum")
+        for o in outs:
+            assert np.array_equal(o.cpu().numpy().view(np.uint64), exp.view(np.uint64))
+    plan.close()
+    for c in comms:
+        c.close()
+
+
 def test_plan_run_host_with_packed_host_buffers(coll):
     """Host-buffer entry point: per-rank host and device buffers laid out back
     to back (copies merge within one allocation) give the same results as the
