@@ -33,7 +33,7 @@
 #include "string.h.cuh"
 #include "omp.h.cuh"
 
-#define NCHUNK 128
+#define NCHUNK 256
 
 __device__ unsigned long long mix64(unsigned long long x) {
     x += 0x9E3779B97F4A7C15ull;
@@ -63,6 +63,7 @@ struct Is {
     int* bstart;   // [nbuckets] first position of each bucket in the send buffer
     int* cnt;      // [range + 1] counting-sort counts, then key ranks
     long* bad;     // [NCHUNK] received keys outside the range, per chunk
+    int* csum;     // [NCHUNK] per-chunk sums of cnt, then their exclusive prefix
 };
 
 __device__ void chunk_range(long n, int c, long* k0, long* k1) {
@@ -88,20 +89,31 @@ __device__ void hist_chunk(long c, void* arg) {
 
 __device__ void bucket_total(long b, void* arg) {
     Is* s = (Is*)arg;
+    const int* h = s->chist + b;
+    const int nb = s->nbuckets;
     int t = 0;
-    for (int c = 0; c < NCHUNK; c++) t += s->chist[c * s->nbuckets + b];
+    for (int c = 0; c < NCHUNK; c += 8) {
+        int v[8];
+        for (int k = 0; k < 8; k++) v[k] = h[(c + k) * nb];
+        for (int k = 0; k < 8; k++) t += v[k];
+    }
     s->hist[b] = t;
 }
 
 // Bucket b: each chunk's counts turned into its write offsets.
 __device__ void bucket_offsets(long b, void* arg) {
     Is* s = (Is*)arg;
+    int* h = s->chist + b;
+    const int nb = s->nbuckets;
     int run = s->bstart[b];
-    for (int c = 0; c < NCHUNK; c++) {
-        int* h = s->chist + c * s->nbuckets + b;
-        const int v = *h;
-        *h = run;
-        run += v;
+    // 8 counts read before any is overwritten: the reads do not wait on the writes
+    for (int c = 0; c < NCHUNK; c += 8) {
+        int v[8];
+        for (int k = 0; k < 8; k++) v[k] = h[(c + k) * nb];
+        for (int k = 0; k < 8; k++) {
+            h[(c + k) * nb] = run;
+            run += v[k];
+        }
     }
 }
 
@@ -117,6 +129,31 @@ __device__ void scatter_chunk(long c, void* arg) {
 }
 
 __device__ void clear_counts(long k, void* arg) { ((Is*)arg)->cnt[k] = 0; }
+
+// Inclusive prefix sum of cnt[0..range] in three passes (chunk sums, their
+// exclusive scan, then each chunk's running sum): the same integers as the
+// serial loop, computed by the whole rank block.
+__device__ void prefix_sum_chunk(long c, void* arg) {
+    Is* s = (Is*)arg;
+    long k0, k1;
+    chunk_range(s->range + 1, (int)c, &k0, &k1);
+    const int* cnt = s->cnt;
+    int t = 0;
+    for (long k = k0; k < k1; k++) t += cnt[k];
+    s->csum[c] = t;
+}
+
+__device__ void prefix_apply_chunk(long c, void* arg) {
+    Is* s = (Is*)arg;
+    long k0, k1;
+    chunk_range(s->range + 1, (int)c, &k0, &k1);
+    int* cnt = s->cnt;
+    int run = s->csum[c];
+    for (long k = k0; k < k1; k++) {
+        run += cnt[k];
+        cnt[k] = run;
+    }
+}
 
 __device__ void count_chunk(long c, void* arg) {
     Is* s = (Is*)arg;
@@ -167,6 +204,7 @@ __device__ int __gpu_main(int argc, char** argv) {
     s->bstart = (int*)malloc(sizeof(int) * nbuckets);
     s->cnt = (int*)malloc(sizeof(int) * (max_key + 1));
     s->bad = (long*)malloc(sizeof(long) * NCHUNK);
+    s->csum = (int*)malloc(sizeof(int) * NCHUNK);
     s->hist = (int*)malloc(sizeof(int) * nbuckets);
     int* hist = s->hist;
     int* ghist = (int*)malloc(sizeof(int) * nbuckets);
@@ -235,7 +273,17 @@ __device__ int __gpu_main(int argc, char** argv) {
         gpumpi_parallel_for(NCHUNK, count_chunk, s);
         long bad = 0;
         for (int c = 0; c < NCHUNK; c++) bad += s->bad[c];
-        for (int k = 0; k < s->range; k++) s->cnt[k + 1] += s->cnt[k];   // cnt[k] = rank of the first key k
+        // cnt[k] = rank of the first key k (inclusive prefix sum; cnt[0] = 0)
+        gpumpi_parallel_for(NCHUNK, prefix_sum_chunk, s);
+        {
+            int run = 0;
+            for (int c = 0; c < NCHUNK; c++) {
+                const int t = s->csum[c];
+                s->csum[c] = run;
+                run += t;
+            }
+        }
+        gpumpi_parallel_for(NCHUNK, prefix_apply_chunk, s);
         unsigned long long h = (unsigned long long)s->nrecv * 0x100000001B3ull + (unsigned long long)bad;
         for (int k = 0; k <= s->range; k += 1 + s->range / 64) h = mix64(h ^ (unsigned long long)s->cnt[k]);
         unsigned long long hsum = 0;
@@ -284,6 +332,7 @@ __device__ int __gpu_main(int argc, char** argv) {
     free(s->bstart);
     free(s->cnt);
     free(s->bad);
+    free(s->csum);
     free(s);
     free(hist);
     free(ghist);
