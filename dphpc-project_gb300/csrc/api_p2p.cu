@@ -612,6 +612,24 @@ __device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source,
 __device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sendtype, int dest,
                             int sendtag, void* recvbuf, int recvcount, MPI_Datatype recvtype,
                             int source, int recvtag, MPI_Comm comm, MPI_Status* status) {
+    {
+        // An eager send completes without the receiver, so the leader may send
+        // first and then receive (the halo exchanges of stencil codes).
+        BlockCtx& b = bctx();
+        u64 sbytes, rbytes;
+        if (small_world_call(b, comm, sendcount, sendtype, &sbytes) && sbytes <= b.eager_bytes &&
+            small_world_call(b, comm, recvcount, recvtype, &rbytes) && dest >= 0 && dest < b.world_size &&
+            sendtag >= 0 && sendtag <= MPI_TAG_UB &&
+            (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
+            (recvtag == MPI_ANY_TAG || (recvtag >= 0 && recvtag <= MPI_TAG_UB))) {
+            if (api_abort_check(b)) return aborted_code();
+            int rc = MPI_SUCCESS;
+            if (p2p_send_small(sendbuf, sbytes, dest, sendtag, &rc)) {
+                if (rc) return rc;
+                return MPI_Recv(recvbuf, recvcount, recvtype, source, recvtag, comm, status);
+            }
+        }
+    }
     MPI_Request rr = MPI_REQUEST_NULL, sr = MPI_REQUEST_NULL;
     int rc = MPI_Irecv(recvbuf, recvcount, recvtype, source, recvtag, comm, &rr);
     if (rc) return rc;
