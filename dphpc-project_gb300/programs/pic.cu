@@ -17,10 +17,11 @@
 // The particle and grid loops run through gpumpi_parallel_for (omp.h.cuh):
 // on the GPU over the rank's whole thread block, in a host build in order.
 // Both give the same bits because nothing depends on the order in which
-// iterations run: particles are cut into `nchunk` fixed chunks of consecutive
-// particles whatever the thread count, energies are summed per chunk and the
-// chunks' sums added in chunk order, particles that leave are listed chunk by
-// chunk (so every buffer keeps the order of a serial loop), and currents are
+// iterations run: particles are dealt into `nchunk` fixed chunks (chunk c holds
+// particles c, c + nchunk, c + 2 nchunk, ...: neighbouring threads read
+// neighbouring particles) whatever the thread count, energies are summed per
+// chunk and the chunks' sums added in chunk order, stayers and leavers are
+// written chunk by chunk at offsets from the chunks' counts, and currents are
 // deposited in 64-bit fixed point (2^-40 units, truncated), whose sums are
 // exact in any order (gpumpi_atomic_add_i64: an atomic add on the GPU, a plain
 // add on the host).
@@ -93,14 +94,13 @@ struct Pic {
     int* ccount;             // [nchunk][9] per chunk: leavers per neighbour, stayers
     long* coff;              // [nchunk][9] write offsets
     double* sbuf[8];         // outgoing particles per neighbour (4 doubles each)
+    double* rbq[8];          // incoming particles per neighbour
+    long roff[9];            // their offsets in the appended run (prefix of the counts)
+    long app_base;           // first index of the appended run
+    long qtot[9];            // leavers per neighbour, stayers (sums over the chunks)
 };
 
 __device__ int gid(const Pic* g, int i, int j) { return (i + 1) + (j + 1) * (g->nx + 2); }
-
-__device__ void chunk_range(long n, int nchunk, int c, long* k0, long* k1) {
-    *k0 = n * c / nchunk;
-    *k1 = n * (c + 1) / nchunk;
-}
 
 __device__ int reserve(Species* s, long need) {
     if (need <= s->cap) return 0;
@@ -196,31 +196,37 @@ __device__ void push_chunk(long c, void* arg) {
     Species* S = &g->sp[g->s];
     const double dt = g->dt;
     const double h = 0.5 * S->qm * dt;
-    long k0, k1;
-    chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
-    for (long k = k0; k < k1; k++) {
+    double* x = S->x;
+    double* y = S->y;
+    double* u = S->u;
+    double* v = S->v;
+    const long n = S->n, step = g->nchunk;
+    const double GXd = (double)g->GX, GYd = (double)g->GY;
+    for (long k = c; k < n; k += step) {
         int i, j;
         double fx, fy;
-        cic(g, S->x[k], S->y[k], &i, &j, &fx, &fy);
+        const double px = x[k], py = y[k];
+        cic(g, px, py, &i, &j, &fx, &fy);
         const double ex = interp(g, g->ex, i, j, fx, fy);
         const double ey = interp(g, g->ey, i, j, fx, fy);
         const double bz = interp(g, g->bz, i, j, fx, fy);
         // Boris: half kick, rotation about z, half kick
-        double um = S->u[k] + h * ex, vm = S->v[k] + h * ey;
+        double um = u[k] + h * ex, vm = v[k] + h * ey;
         const double t = h * bz;
         const double sfac = 2.0 * t / (1.0 + t * t);
         const double up_ = um + vm * t, vp_ = vm - um * t;
         um = um + vp_ * sfac;
         vm = vm - up_ * sfac;
-        S->u[k] = um + h * ex;
-        S->v[k] = vm + h * ey;
-        double nxp = S->x[k] + S->u[k] * dt, nyp = S->y[k] + S->v[k] * dt;
-        if (nxp < 0.0) nxp += (double)g->GX;
-        if (nxp >= (double)g->GX) nxp -= (double)g->GX;
-        if (nyp < 0.0) nyp += (double)g->GY;
-        if (nyp >= (double)g->GY) nyp -= (double)g->GY;
-        S->x[k] = nxp;
-        S->y[k] = nyp;
+        const double un = um + h * ex, vn = vm + h * ey;
+        u[k] = un;
+        v[k] = vn;
+        double nxp = px + un * dt, nyp = py + vn * dt;
+        if (nxp < 0.0) nxp += GXd;
+        if (nxp >= GXd) nxp -= GXd;
+        if (nyp < 0.0) nyp += GYd;
+        if (nyp >= GYd) nyp -= GYd;
+        x[k] = nxp;
+        y[k] = nyp;
     }
 }
 
@@ -229,11 +235,13 @@ __device__ void classify_chunk(long c, void* arg) {
     Pic* g = (Pic*)arg;
     Species* S = &g->sp[g->s];
     int* cnt = g->ccount + c * 9;
-    for (int q = 0; q < 9; q++) cnt[q] = 0;
-    long k0, k1;
-    chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
-    for (long k = k0; k < k1; k++) {
-        const int cx = (int)S->x[k] / g->nx, cy = (int)S->y[k] / g->ny;
+    int loc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const double* x = S->x;
+    const double* y = S->y;
+    signed char* dest = g->dest;
+    const long n = S->n, step = g->nchunk;
+    for (long k = c; k < n; k += step) {
+        const int cx = (int)x[k] / g->nx, cy = (int)y[k] / g->ny;
         int dx = cx - g->bx, dy = cy - g->by;
         if (dx > 1) dx -= g->PX;
         if (dx < -1) dx += g->PX;
@@ -244,34 +252,43 @@ __device__ void classify_chunk(long c, void* arg) {
             q = (dy + 1) * 3 + (dx + 1);
             if (q > 4) q--;
         }
-        g->dest[k] = (signed char)q;
-        cnt[q < 0 ? 8 : q]++;
+        dest[k] = (signed char)q;
+        loc[q < 0 ? 8 : q]++;
     }
+    for (int q = 0; q < 9; q++) cnt[q] = loc[q];
 }
 
 // Leavers go to their neighbour's buffer, stayers to the compacted arrays,
-// each at the offsets of its chunk (so the order is the particle order).
+// each at the offsets of its chunk (chunk-major order, the same in every build).
 __device__ void scatter_chunk(long c, void* arg) {
     Pic* g = (Pic*)arg;
     Species* S = &g->sp[g->s];
     long off[9];
     for (int q = 0; q < 9; q++) off[q] = g->coff[c * 9 + q];
-    long k0, k1;
-    chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
-    for (long k = k0; k < k1; k++) {
-        const int q = g->dest[k];
+    const double* x = S->x;
+    const double* y = S->y;
+    const double* u = S->u;
+    const double* v = S->v;
+    double* ax = S->ax;
+    double* ay = S->ay;
+    double* au = S->au;
+    double* av = S->av;
+    const signed char* dest = g->dest;
+    const long n = S->n, step = g->nchunk;
+    for (long k = c; k < n; k += step) {
+        const int q = dest[k];
         if (q < 0) {
             const long w = off[8]++;
-            S->ax[w] = S->x[k];
-            S->ay[w] = S->y[k];
-            S->au[w] = S->u[k];
-            S->av[w] = S->v[k];
+            ax[w] = x[k];
+            ay[w] = y[k];
+            au[w] = u[k];
+            av[w] = v[k];
         } else {
             double* d = g->sbuf[q] + 4 * off[q]++;
-            d[0] = S->x[k];
-            d[1] = S->y[k];
-            d[2] = S->u[k];
-            d[3] = S->v[k];
+            d[0] = x[k];
+            d[1] = y[k];
+            d[2] = u[k];
+            d[3] = v[k];
         }
     }
 }
@@ -285,6 +302,41 @@ __device__ void deposit_fixed(const Pic* g, long long* f, int i, int j, double f
     gpumpi_atomic_add_i64(&f[gid(g, i + 1, j + 1)], (long long)(val * fx * fy * FIX_ONE));
 }
 
+// Destination q (0..7 a neighbour, 8 the stayers): every chunk's write offset
+// is the sum of the earlier chunks' counts.  Eight counts are read before any
+// offset is written, so the reads do not wait on the writes.
+__device__ void chunk_offsets_q(long q, void* arg) {
+    Pic* g = (Pic*)arg;
+    const int nch = g->nchunk;
+    const int* cnt = g->ccount;
+    long* off = g->coff;
+    long run = 0;
+    for (int c = 0; c < nch; c += 8) {
+        const int m = nch - c < 8 ? nch - c : 8;
+        int v[8];
+        for (int k = 0; k < m; k++) v[k] = cnt[(c + k) * 9 + (int)q];
+        for (int k = 0; k < m; k++) {
+            off[(c + k) * 9 + (int)q] = run;
+            run += v[k];
+        }
+    }
+    g->qtot[q] = run;
+}
+
+// Incoming particle i (neighbour-major order) appended after the stayers.
+__device__ void append_particle(long i, void* arg) {
+    Pic* g = (Pic*)arg;
+    Species* S = &g->sp[g->s];
+    int q = 0;
+    while (i >= g->roff[q + 1]) q++;
+    const double* d = g->rbq[q] + 4 * (i - g->roff[q]);
+    const long k = g->app_base + i;
+    S->x[k] = d[0];
+    S->y[k] = d[1];
+    S->u[k] = d[2];
+    S->v[k] = d[3];
+}
+
 __device__ void clear_current_cell(long k, void* arg) {
     Pic* g = (Pic*)arg;
     g->ajx[k] = 0;
@@ -296,14 +348,18 @@ __device__ void deposit_chunk(long c, void* arg) {
     Pic* g = (Pic*)arg;
     for (int s = 0; s < NSPEC; s++) {
         const Species* S = &g->sp[s];
-        long k0, k1;
-        chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
-        for (long k = k0; k < k1; k++) {
+        const double* x = S->x;
+        const double* y = S->y;
+        const double* u = S->u;
+        const double* v = S->v;
+        const double qw = S->qw;
+        const long n = S->n, step = g->nchunk;
+        for (long k = c; k < n; k += step) {
             int i, j;
             double fx, fy;
-            cic(g, S->x[k], S->y[k], &i, &j, &fx, &fy);
-            deposit_fixed(g, g->ajx, i, j, fx, fy, S->qw * S->u[k]);
-            deposit_fixed(g, g->ajy, i, j, fx, fy, S->qw * S->v[k]);
+            cic(g, x[k], y[k], &i, &j, &fx, &fy);
+            deposit_fixed(g, g->ajx, i, j, fx, fy, qw * u[k]);
+            deposit_fixed(g, g->ajy, i, j, fx, fy, qw * v[k]);
         }
     }
 }
@@ -338,10 +394,11 @@ __device__ void energy_chunk(long c, void* arg) {
     double* e = g->part + c * 4;
     for (int s = 0; s < NSPEC; s++) {
         const Species* S = &g->sp[s];
-        long k0, k1;
-        chunk_range(S->n, g->nchunk, (int)c, &k0, &k1);
+        const double* u = S->u;
+        const double* v = S->v;
+        const long n = S->n, step = g->nchunk;
         double ke = 0.0;
-        for (long k = k0; k < k1; k++) ke += S->u[k] * S->u[k] + S->v[k] * S->v[k];
+        for (long k = c; k < n; k += step) ke += u[k] * u[k] + v[k] * v[k];
         e[s] = ke;
     }
     e[2] = 0.0;
@@ -482,15 +539,9 @@ __device__ int __gpu_main(int argc, char** argv) {
             }
             gpumpi_parallel_for(nchunk, classify_chunk, g);
             int scnt[8], rcnt[8];
-            long stay = 0;
-            for (int q = 0; q < 8; q++) scnt[q] = 0;
-            for (int c = 0; c < nchunk; c++)
-                for (int q = 0; q < 9; q++) {
-                    const int v = g->ccount[c * 9 + q];
-                    g->coff[c * 9 + q] = q == 8 ? stay : (long)scnt[q];
-                    if (q == 8) stay += v;
-                    else scnt[q] += v;
-                }
+            gpumpi_parallel_for(9, chunk_offsets_q, g);
+            for (int q = 0; q < 8; q++) scnt[q] = (int)g->qtot[q];
+            const long stay = g->qtot[8];
             for (int q = 0; q < 8; q++) g->sbuf[q] = (double*)malloc(sizeof(double) * 4 * (scnt[q] > 0 ? scnt[q] : 1));
             gpumpi_parallel_for(nchunk, scatter_chunk, g);
             // the compacted arrays become the species' arrays (with their capacity)
@@ -520,15 +571,16 @@ __device__ int __gpu_main(int argc, char** argv) {
             }
             if (MPI_Waitall(16, rq, MPI_STATUSES_IGNORE) != MPI_SUCCESS) status = 1;
             if (reserve(S, S->n + nin)) status = 1;
-            for (int q = 0; q < 8 && !status; q++)
-                for (int m = 0; m < rcnt[q]; m++) {
-                    const double* d = rbuf[q] + 4 * m;
-                    const long k = S->n++;
-                    S->x[k] = d[0];
-                    S->y[k] = d[1];
-                    S->u[k] = d[2];
-                    S->v[k] = d[3];
+            if (!status) {
+                g->roff[0] = 0;
+                for (int q = 0; q < 8; q++) {
+                    g->rbq[q] = rbuf[q];
+                    g->roff[q + 1] = g->roff[q] + rcnt[q];
                 }
+                g->app_base = S->n;
+                gpumpi_parallel_for(nin, append_particle, g);
+                S->n += nin;
+            }
             for (int q = 0; q < 8; q++) {
                 free(g->sbuf[q]);
                 free(rbuf[q]);
