@@ -3,6 +3,7 @@
 // layout in HBM, co-residency check (main.cu:189-209, done here with the
 // cooperative-launch occupancy query), launch, output drain and exit status.
 #include <cuda_runtime.h>
+#include <errno.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -10,6 +11,7 @@
 #include <time.h>
 
 #include <string>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -318,6 +320,93 @@ static bool allow_dynamic_smem(const void* kernel, size_t smem) {
     return true;
 }
 
+// ------------------------------------------------------------------ host calls
+// Files the ranks of one program opened through their HostCall slots.
+struct HostFiles {
+    std::vector<FILE*> f;
+    ~HostFiles() {
+        for (FILE* fp : f)
+            if (fp) fclose(fp);
+    }
+    FILE* get(long long h) const { return h >= 0 && h < (long long)f.size() ? f[(size_t)h] : nullptr; }
+};
+
+// Answer every posted request; returns how many were answered.
+static int service_host_calls(HostCall* hc, int n, HostFiles& files) {
+    int served = 0;
+    for (int r = 0; r < n; r++) {
+        volatile u32* state = &hc[r].state;
+        if (*state != 1u) continue;
+        std::atomic_thread_fence(std::memory_order_acquire);
+        HostCall& c = hc[r];
+        long long ret = -1;
+        int err = 0;
+        u32 len = 0;
+        errno = 0;
+        FILE* fp = files.get(c.a[0]);
+        switch (c.op) {
+            case HC_OPEN: {
+                c.data[HOSTCALL_DATA - 1] = 0;
+                const char* path = c.data;
+                const size_t pl = strlen(path);
+                const char* mode = pl + 1 < HOSTCALL_DATA ? c.data + pl + 1 : "r";
+                FILE* nf = fopen(path, mode);
+                if (nf) {
+                    files.f.push_back(nf);
+                    ret = (long long)files.f.size() - 1;
+                }
+                break;
+            }
+            case HC_CLOSE:
+                if (fp) {
+                    ret = fclose(fp) == 0 ? 0 : -1;
+                    files.f[(size_t)c.a[0]] = nullptr;
+                } else {
+                    errno = EBADF;
+                }
+                break;
+            case HC_WRITE:
+                if (fp && c.len <= HOSTCALL_DATA) ret = (long long)fwrite(c.data, 1, c.len, fp);
+                else errno = EBADF;
+                break;
+            case HC_READ:
+                if (fp) {
+                    const size_t want = c.a[1] > 0 && c.a[1] < HOSTCALL_DATA ? (size_t)c.a[1] : HOSTCALL_DATA;
+                    const size_t got = fread(c.data, 1, want, fp);
+                    ret = (long long)got;
+                    len = (u32)got;
+                } else {
+                    errno = EBADF;
+                }
+                break;
+            case HC_FLUSH:
+                ret = fp && fflush(fp) == 0 ? 0 : -1;
+                break;
+            case HC_SEEK:
+                ret = fp && fseek(fp, (long)c.a[1], (int)c.a[2]) == 0 ? 0 : -1;
+                break;
+            case HC_TELL:
+                ret = fp ? (long long)ftell(fp) : -1;
+                break;
+            case HC_REMOVE:
+                c.data[HOSTCALL_DATA - 1] = 0;
+                ret = remove(c.data) == 0 ? 0 : -1;
+                break;
+            default:
+                errno = ENOSYS;
+                break;
+        }
+        if (ret < 0) err = errno ? errno : EIO;
+        c.ret = ret;
+        c.err = err;
+        c.len = len;
+        std::atomic_thread_fence(std::memory_order_release);
+        *state = 2u;
+        served++;
+    }
+    return served;
+}
+
 // Choose threads per rank: the largest of 256/128/64 that keeps every rank
 // resident, given the kernel's register and shared-memory use.
 size_t pick_rank_smem(const void* kernel, int T, int need) {
@@ -474,6 +563,15 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     hj.job.argv = (char**)dargs;
     hj.job.threads = T;
 
+    // host-call slots (file I/O of the program), mapped into the device
+    HostCall* hcall = nullptr;
+    HCHECK(cudaHostAlloc((void**)&hcall, sizeof(HostCall) * (size_t)n, cudaHostAllocMapped));
+    memset(hcall, 0, sizeof(HostCall) * (size_t)n);
+    HostCall* dhcall = nullptr;
+    HCHECK(cudaHostGetDevicePointer((void**)&dhcall, hcall, 0));
+    hj.job.hcall = dhcall;
+    HostFiles files;
+
     // one job, one slot per rank
     std::vector<int> slots(2 * (size_t)n);
     for (int r = 0; r < n; r++) {
@@ -518,7 +616,7 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
             fflush(stderr);
             _exit(3);
         }
-        usleep(200);
+        if (service_host_calls(hcall, n, files) == 0) usleep(20);
     }
     HCHECK(cudaStreamSynchronize(st));
 
@@ -536,5 +634,6 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     cudaFree(dslots);
     cudaFree(dargs);
     cudaFree(base);
+    cudaFreeHost(hcall);
     return res.exit_code;
 }

@@ -14,16 +14,122 @@
 
 using namespace gm;
 
+constexpr int FILE_BUF = HOSTCALL_DATA;
+
 struct gpumpi_file_impl {
-    int stream;   // 1 stdout, 2 stderr, 0 stdin
+    int stream;        // 1 stdout, 2 stderr, 0 stdin, 3 a host file opened through the launcher
+    int eof;
+    int wlen;          // bytes buffered for writing
+    int rpos, rlen;    // unread window of the read buffer
+    long long handle;  // the launcher's handle of a host file
+    char* wbuf;        // [FILE_BUF] (host files only)
+    char* rbuf;        // [FILE_BUF]
 };
 
-__device__ gpumpi_file_impl gm_file_stdout = {1};
-__device__ gpumpi_file_impl gm_file_stderr = {2};
-__device__ gpumpi_file_impl gm_file_stdin = {0};
+__device__ gpumpi_file_impl gm_file_stdout = {1, 0, 0, 0, 0, -1, nullptr, nullptr};
+__device__ gpumpi_file_impl gm_file_stderr = {2, 0, 0, 0, 0, -1, nullptr, nullptr};
+__device__ gpumpi_file_impl gm_file_stdin = {0, 0, 0, 0, 0, -1, nullptr, nullptr};
 __device__ __gpu_FILE* __gpu_stdout = &gm_file_stdout;
 __device__ __gpu_FILE* __gpu_stderr = &gm_file_stderr;
 __device__ __gpu_FILE* __gpu_stdin = &gm_file_stdin;
+
+// ---------------------------------------------------------------- host files
+// The rank's leader calls the launcher through its HostCall slot (mapped host
+// memory, system-scope release/acquire).  Returns the answer's ret; on failure
+// (ret < 0) errno is set.  Without a host service (collective API, serving)
+// every call fails with ENOENT, as fopen did before there was one.
+static __device__ long long host_call(u32 op, long long a0, long long a1, long long a2, const void* in,
+                                      u32 in_len, void* out, u32 out_cap, u32* out_len) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    if (out_len) *out_len = 0;
+    if (!j->hcall) {
+        b.priv->errno_v = 2;   // ENOENT
+        return -1;
+    }
+    HostCall* h = &j->hcall[b.rank];
+    h->op = op;
+    h->a[0] = a0;
+    h->a[1] = a1;
+    h->a[2] = a2;
+    h->len = in_len;
+    for (u32 i = 0; i < in_len; i++) h->data[i] = ((const char*)in)[i];
+    __threadfence_system();
+    asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(&h->state), "r"(1u) : "memory");
+    const u64 t0 = gtime();
+    unsigned ns = 256;
+    for (;;) {
+        u32 st;
+        asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(st) : "l"(&h->state) : "memory");
+        if (st == 2) break;
+        if (ld_relaxed_int(&j->status[0]) != 0) {
+            b.priv->errno_v = 5;   // EIO
+            return -1;
+        }
+        if (gtime() - t0 > j->timeout_ns) {
+            job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "host file call timed out");
+            b.priv->errno_v = 5;
+            return -1;
+        }
+        __nanosleep(ns);
+        if (ns < 8192) ns <<= 1;
+    }
+    const volatile HostCall* vh = h;
+    const long long ret = vh->ret;
+    const int err = vh->err;
+    u32 n = vh->len;
+    if (n > out_cap) n = out_cap;
+    for (u32 i = 0; i < n; i++) ((char*)out)[i] = vh->data[i];
+    if (out_len) *out_len = n;
+    h->state = 0u;   // the next request's release orders this store before its own
+    if (ret < 0) b.priv->errno_v = err;
+    return ret;
+}
+
+static __device__ int file_flush_write(gpumpi_file_impl* f) {
+    int rc = 0;
+    if (f->wlen > 0) {
+        const long long r = host_call(HC_WRITE, f->handle, 0, 0, f->wbuf, (u32)f->wlen, nullptr, 0, nullptr);
+        if (r != f->wlen) rc = -1;
+        f->wlen = 0;
+    }
+    return rc;
+}
+
+static __device__ int file_write(gpumpi_file_impl* f, const char* p, u64 n) {
+    if (f->rpos < f->rlen) {   // writing after reading: drop the unread window, position at it
+        host_call(HC_SEEK, f->handle, -(long long)(f->rlen - f->rpos), 1, nullptr, 0, nullptr, 0, nullptr);
+        f->rpos = f->rlen = 0;
+    }
+    u64 done = 0;
+    while (done < n) {
+        u64 k = (u64)(FILE_BUF - f->wlen);
+        if (k > n - done) k = n - done;
+        for (u64 i = 0; i < k; i++) f->wbuf[f->wlen + i] = p[done + i];
+        f->wlen += (int)k;
+        done += k;
+        if (f->wlen == FILE_BUF && file_flush_write(f)) return -1;
+    }
+    return 0;
+}
+
+// Refill the read buffer; 0 bytes: end of file (or an error).
+static __device__ int file_fill(gpumpi_file_impl* f) {
+    if (file_flush_write(f)) return 0;
+    u32 got = 0;
+    const long long r = host_call(HC_READ, f->handle, FILE_BUF, 0, nullptr, 0, f->rbuf, FILE_BUF, &got);
+    f->rpos = 0;
+    f->rlen = r > 0 ? (int)got : 0;
+    if (f->rlen == 0) f->eof = 1;
+    return f->rlen;
+}
+
+static __device__ int file_getc(gpumpi_file_impl* f) {
+    if (f->rpos == f->rlen && file_fill(f) == 0) return -1;
+    return (unsigned char)f->rbuf[f->rpos++];
+}
+
+static __device__ bool host_file(const __gpu_FILE* f) { return f && f->stream == 3; }
 
 // ---------------------------------------------------------------- stdio
 static __device__ int emit(int stream, const char* fmt, va_list ap) {
@@ -60,6 +166,28 @@ __device__ int __gpu_printf(const char* format, ...) {
 
 __device__ int __gpu_vfprintf(__gpu_FILE* stream, const char* format, va_list ap) {
     if (!stream || stream->stream == 0) return -1;
+    if (host_file(stream)) {
+        Job* j = bctx().job;
+        char line[OUT_LINE_MAX];
+        va_list ap2;
+        va_copy(ap2, ap);
+        const int n = gmfmt::vformat(line, sizeof(line), format, ap);
+        int rc;
+        if (n < (int)sizeof(line)) {
+            rc = file_write(stream, line, (u64)n);
+        } else {
+            char* big = (char*)heap_alloc(&j->heap, (u64)n + 1);
+            if (!big) {
+                va_end(ap2);
+                return -1;
+            }
+            gmfmt::vformat(big, (size_t)n + 1, format, ap2);
+            rc = file_write(stream, big, (u64)n);
+            heap_free(&j->heap, big);
+        }
+        va_end(ap2);
+        return rc ? -1 : n;
+    }
     return emit(stream->stream, format, ap);
 }
 
@@ -99,6 +227,7 @@ __device__ int __gpu_fputs(const char* s, __gpu_FILE* stream) {
     if (!stream || stream->stream == 0) return -1;
     int n = 0;
     while (s[n]) n++;
+    if (host_file(stream)) return file_write(stream, s, (u64)n) ? -1 : n;
     out_write(bctx().job, stream->stream, s, n);
     return n;
 }
@@ -112,6 +241,7 @@ __device__ int __gpu_puts(const char* s) {
 __device__ int __gpu_fputc(int c, __gpu_FILE* stream) {
     if (!stream || stream->stream == 0) return -1;
     char ch = (char)c;
+    if (host_file(stream)) return file_write(stream, &ch, 1) ? -1 : (unsigned char)ch;
     out_write(bctx().job, stream->stream, &ch, 1);
     return (unsigned char)ch;
 }
@@ -120,49 +250,142 @@ __device__ int __gpu_putchar(int c) { return __gpu_fputc(c, __gpu_stdout); }
 
 __device__ size_t __gpu_fwrite(const void* ptr, size_t size, size_t nmemb, __gpu_FILE* stream) {
     if (!stream || stream->stream == 0) return 0;
+    if (host_file(stream)) return file_write(stream, (const char*)ptr, (u64)size * nmemb) ? 0 : nmemb;
     out_write(bctx().job, stream->stream, (const char*)ptr, (int)(size * nmemb));
     return nmemb;
 }
 
 __device__ int __gpu_fflush(__gpu_FILE* stream) {
-    (void)stream;
-    return 0;
+    if (!host_file(stream)) return 0;
+    if (file_flush_write(stream)) return -1;
+    return host_call(HC_FLUSH, stream->handle, 0, 0, nullptr, 0, nullptr, 0, nullptr) < 0 ? -1 : 0;
 }
 
-// Files are not reachable from the device in this runtime: fopen fails
-// cleanly (the reference's stubs trapped, gpu_libs/gpu_libc/stdio.cu:21-76).
+// Files are opened, read and written by the launcher on the rank's behalf
+// (host_call); each open file keeps a write buffer and a read buffer of
+// HOSTCALL_DATA bytes in the device heap.  The reference's stubs trapped
+// (gpu_libs/gpu_libc/stdio.cu:21-76) and its host-side processor was empty
+// (gpu_libs/gpu_main/libc_processor.cu:3-5).
 __device__ __gpu_FILE* __gpu_fopen(const char* pathname, const char* mode) {
-    (void)pathname;
-    (void)mode;
-    bctx().priv->errno_v = 2;  // ENOENT
-    return nullptr;
+    if (!pathname || !mode) return nullptr;
+    char req[512];
+    u32 n = 0;
+    for (const char* p = pathname; *p; p++) {
+        if (n + 2 >= sizeof(req)) {
+            bctx().priv->errno_v = 36;   // ENAMETOOLONG
+            return nullptr;
+        }
+        req[n++] = *p;
+    }
+    req[n++] = 0;
+    for (const char* p = mode; *p && n + 1 < sizeof(req); p++) req[n++] = *p;
+    req[n++] = 0;
+    Job* j = bctx().job;
+    gpumpi_file_impl* f = (gpumpi_file_impl*)heap_alloc(&j->heap, sizeof(gpumpi_file_impl) + 2 * FILE_BUF);
+    if (!f) {
+        bctx().priv->errno_v = 12;   // ENOMEM
+        return nullptr;
+    }
+    const long long h = host_call(HC_OPEN, 0, 0, 0, req, n, nullptr, 0, nullptr);
+    if (h < 0) {
+        heap_free(&j->heap, f);
+        return nullptr;
+    }
+    f->stream = 3;
+    f->eof = 0;
+    f->wlen = 0;
+    f->rpos = f->rlen = 0;
+    f->handle = h;
+    f->wbuf = (char*)(f + 1);
+    f->rbuf = f->wbuf + FILE_BUF;
+    return f;
 }
-__device__ int __gpu_fclose(__gpu_FILE* stream) { return stream ? 0 : -1; }
+
+__device__ int __gpu_fclose(__gpu_FILE* stream) {
+    if (!stream) return -1;
+    if (!host_file(stream)) return 0;
+    int rc = file_flush_write(stream);
+    if (host_call(HC_CLOSE, stream->handle, 0, 0, nullptr, 0, nullptr, 0, nullptr) < 0) rc = -1;
+    heap_free(&bctx().job->heap, stream);
+    return rc;
+}
+
 __device__ char* __gpu_fgets(char* s, int size, __gpu_FILE* stream) {
-    (void)s;
-    (void)size;
-    (void)stream;
-    return nullptr;
+    if (!host_file(stream) || size <= 0) return nullptr;
+    int n = 0;
+    while (n < size - 1) {
+        const int c = file_getc(stream);
+        if (c < 0) break;
+        s[n++] = (char)c;
+        if (c == '\n') break;
+    }
+    if (n == 0) return nullptr;
+    s[n] = 0;
+    return s;
 }
+
 __device__ int __gpu_fgetc(__gpu_FILE* stream) {
-    (void)stream;
-    return -1;
+    if (!host_file(stream)) return -1;
+    return file_getc(stream);
 }
+
 __device__ int __gpu_feof(__gpu_FILE* stream) {
-    (void)stream;
-    return 1;
+    if (!host_file(stream)) return 1;
+    return stream->eof && stream->rpos == stream->rlen;
 }
+
 __device__ int __gpu_fscanf(__gpu_FILE* stream, const char* format, ...) {
     (void)stream;
     (void)format;
     return -1;
 }
+
 __device__ size_t __gpu_fread(void* ptr, size_t size, size_t nmemb, __gpu_FILE* stream) {
-    (void)ptr;
-    (void)size;
-    (void)nmemb;
-    (void)stream;
-    return 0;
+    if (!host_file(stream) || size == 0) return 0;
+    const u64 want = (u64)size * nmemb;
+    char* d = (char*)ptr;
+    u64 got = 0;
+    while (got < want) {
+        if (stream->rpos == stream->rlen && file_fill(stream) == 0) break;
+        u64 k = (u64)(stream->rlen - stream->rpos);
+        if (k > want - got) k = want - got;
+        for (u64 i = 0; i < k; i++) d[got + i] = stream->rbuf[stream->rpos + i];
+        stream->rpos += (int)k;
+        got += k;
+    }
+    return got / size;
+}
+
+__device__ int __gpu_fseek(__gpu_FILE* stream, long offset, int whence) {
+    if (!host_file(stream)) return -1;
+    if (file_flush_write(stream)) return -1;
+    long long off = offset;
+    if (whence == 1) off -= (long long)(stream->rlen - stream->rpos);   // SEEK_CUR: from the user's position
+    stream->rpos = stream->rlen = 0;
+    stream->eof = 0;
+    return host_call(HC_SEEK, stream->handle, off, whence, nullptr, 0, nullptr, 0, nullptr) < 0 ? -1 : 0;
+}
+
+__device__ long __gpu_ftell(__gpu_FILE* stream) {
+    if (!host_file(stream)) return -1;
+    const long long pos = host_call(HC_TELL, stream->handle, 0, 0, nullptr, 0, nullptr, 0, nullptr);
+    if (pos < 0) return -1;
+    return (long)(pos - (stream->rlen - stream->rpos) + stream->wlen);
+}
+
+__device__ void __gpu_rewind(__gpu_FILE* stream) {
+    if (__gpu_fseek(stream, 0, 0) == 0) stream->eof = 0;
+}
+
+__device__ int __gpu_remove(const char* pathname) {
+    u32 n = 0;
+    char req[512];
+    for (const char* p = pathname; *p; p++) {
+        if (n + 1 >= sizeof(req)) return -1;
+        req[n++] = *p;
+    }
+    req[n++] = 0;
+    return host_call(HC_REMOVE, 0, 0, 0, req, n, nullptr, 0, nullptr) < 0 ? -1 : 0;
 }
 
 // ---------------------------------------------------------------- memory

@@ -245,6 +245,8 @@ __host__ size_t heap_ctl_bytes();
 __host__ void heap_set_ctl(Heap& h, char* ctl);
 
 // One MPI job (a converted program instance with its own MPI_COMM_WORLD).
+struct HostCall;
+
 struct Job {
     int id;
     int nranks;
@@ -277,7 +279,36 @@ struct Job {
     int* retvals;                 // [nranks]
     char* err_msg;                // 256 bytes
     u64 t0_ns;                    // %globaltimer at launch
+    HostCall* hcall;              // [nranks] mapped host memory, or null: no host service
 };
+
+// Device -> host calls (file I/O of converted programs).  One slot per rank in
+// host memory mapped into the device: the rank's leader fills the request,
+// publishes state = 1 with a system-scope release, and waits (bounded) for
+// the launcher to answer with state = 2.  The launcher polls the slots while
+// the kernel runs.
+constexpr int HOSTCALL_DATA = 4096;
+enum HostCallOp : u32 {
+    HC_OPEN = 1,     // data: path '\0' mode '\0' -> ret: handle
+    HC_CLOSE = 2,    // a0: handle
+    HC_WRITE = 3,    // a0: handle, data[len] -> ret: bytes written
+    HC_READ = 4,     // a0: handle, a1: bytes wanted (<= HOSTCALL_DATA) -> data[len], ret: bytes read
+    HC_FLUSH = 5,    // a0: handle
+    HC_SEEK = 6,     // a0: handle, a1: offset, a2: whence
+    HC_TELL = 7,     // a0: handle -> ret: position
+    HC_REMOVE = 8,   // data: path
+};
+struct alignas(64) HostCall {
+    u32 state;       // 0 idle, 1 posted by the device, 2 answered by the host
+    u32 op;
+    long long a[3];
+    long long ret;   // < 0: failed, err holds errno
+    int err;
+    u32 len;         // bytes in data (request or answer)
+    char pad[16];
+    char data[HOSTCALL_DATA];
+};
+static_assert(offsetof(HostCall, data) % 16 == 0, "HostCall data alignment");
 
 // Where a thread block finds its job: slot -> (job, rank).
 struct Launch {

@@ -44,6 +44,10 @@ __device__ int __gpu_feof(__gpu_FILE* stream);
 __device__ int __gpu_fscanf(__gpu_FILE* stream, const char* format, ...);
 __device__ size_t __gpu_fwrite(const void* ptr, size_t size, size_t nmemb, __gpu_FILE* stream);
 __device__ size_t __gpu_fread(void* ptr, size_t size, size_t nmemb, __gpu_FILE* stream);
+__device__ int __gpu_fseek(__gpu_FILE* stream, long offset, int whence);
+__device__ long __gpu_ftell(__gpu_FILE* stream);
+__device__ void __gpu_rewind(__gpu_FILE* stream);
+__device__ int __gpu_remove(const char* pathname);
 
 // stdlib
 __device__ void* __gpu_malloc(size_t size);

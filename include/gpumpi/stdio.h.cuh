@@ -33,3 +33,12 @@
 #define puts __gpu_puts
 #define fwrite __gpu_fwrite
 #define fread __gpu_fread
+#define fseek __gpu_fseek
+#define ftell __gpu_ftell
+#define rewind __gpu_rewind
+#define remove __gpu_remove
+#ifndef SEEK_SET
+#define SEEK_SET 0
+#define SEEK_CUR 1
+#define SEEK_END 2
+#endif

@@ -19,7 +19,7 @@ CASES = os.path.join(ROOT, "tests", "convert_cases")
 ORACLE = os.path.join(ROOT, "oracle")
 REF = "/root/reference"
 NVCC = "/usr/local/cuda/bin/nvcc"
-CASE_OPTS = {"globals": 0, "ring": 0, "coalesce": 3}
+CASE_OPTS = {"globals": 0, "ring": 0, "coalesce": 3, "fileio": 0}
 
 
 @pytest.fixture(scope="module")
@@ -221,8 +221,9 @@ def test_unsupported_forms_are_reported(conv):
 # ---------------------------------------------------------------- semantics on the oracle
 
 
-def _run(exe, n, timeout=120):
-    r = subprocess.run([exe, "---gpumpi", "-n", str(n)], capture_output=True, text=True, timeout=timeout)
+def _run(exe, n, timeout=120, cwd=None):
+    r = subprocess.run([exe, "---gpumpi", "-n", str(n)], capture_output=True, text=True, timeout=timeout,
+                       cwd=cwd)
     assert r.returncode == 0, r.stderr[-2000:]
     return r.stdout
 
@@ -254,11 +255,13 @@ def case_builds(oracle_built, tmp_path_factory):
 
 @pytest.mark.parametrize("name", sorted(CASE_OPTS))
 @pytest.mark.parametrize("ranks", [1, 3, 8])
-def test_converted_cases_match_the_original_on_the_oracle(case_builds, name, ranks):
+def test_converted_cases_match_the_original_on_the_oracle(case_builds, name, ranks, tmp_path):
     orig, conv_exe, _ = case_builds[name]
-    a = _run(orig, ranks)
+    (tmp_path / "a").mkdir()
+    (tmp_path / "b").mkdir()
+    a = _run(orig, ranks, cwd=str(tmp_path / "a"))   # fileio.c writes in its working directory
     assert a.strip()
-    assert _run(conv_exe, ranks) == a
+    assert _run(conv_exe, ranks, cwd=str(tmp_path / "b")) == a
 
 
 @pytest.mark.skipif(not os.path.exists(NVCC), reason="nvcc absent")

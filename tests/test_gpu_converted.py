@@ -2,7 +2,8 @@
 
 The converter's test programs (tests/convert_cases/*.c) are converted and
 compiled on this machine, run by the device runtime, and must print what the
-unmodified C program prints on the hostmpi oracle.  When the converted forms
+unmodified C program prints on the hostmpi oracle (fileio.c writes, reads,
+seeks and removes files through the launcher's host calls).  When the converted forms
 of the reference's own programs are present (oracle/_ref/conv, made from the
 reference tree by `make -C oracle -f ref.mk conv`), those run too: cpi.c must
 print the golden lines, global_var.c must report no error, and NPB IS and DT
@@ -21,7 +22,7 @@ CASES = os.path.join(ROOT, "tests", "convert_cases")
 ORACLE = os.path.join(ROOT, "oracle")
 GPUMPICC = os.path.join(ROOT, "dphpc-project_gb300", "gpumpicc.py")
 CONV = os.path.join(ORACLE, "_ref", "conv")
-CASE_OPTS = {"globals": 0, "ring": 0, "coalesce": 3}
+CASE_OPTS = {"globals": 0, "ring": 0, "coalesce": 3, "fileio": 0}
 GPU_OPTS = ["--timeout-ms", "20000", "--max-seconds", "200"]
 NPBDEFS = ['-DNPBVERSION="3.4.1"', '-DCOMPILETIME="n/a"', '-DMPICC="gcc"', '-DCFLAGS="-O2"', '-DCLINK="gcc"',
            '-DCLINKFLAGS=""', '-DCMPI_LIB="hostmpi"', '-DCMPI_INC=""']
@@ -38,8 +39,8 @@ def _gpumpicc(args, cwd):
     _check(r)
 
 
-def _run(cmd, timeout=300):
-    r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+def _run(cmd, timeout=300, cwd=None):
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout, cwd=cwd)
     _check(r)
     return r.stdout
 
@@ -62,11 +63,16 @@ def cases(gpu_built, tmp_path_factory):
 
 @pytest.mark.parametrize("name", sorted(CASE_OPTS))
 @pytest.mark.parametrize("ranks", [1, 3, 8, 64])
-def test_gpu_converted_case_matches_the_original_on_hostmpi(cases, name, ranks):
+def test_gpu_converted_case_matches_the_original_on_hostmpi(cases, name, ranks, tmp_path):
     orig, gpu = cases[name]
-    want = _run([orig, "---gpumpi", "-n", str(ranks)])
-    got = _run([gpu, "---gpumpi", "-n", str(ranks), *GPU_OPTS])
+    (tmp_path / "host").mkdir()
+    (tmp_path / "gpu").mkdir()
+    # fileio.c creates, reads and removes files in its working directory (on
+    # the GPU through the launcher's host calls)
+    want = _run([orig, "---gpumpi", "-n", str(ranks)], cwd=str(tmp_path / "host"))
+    got = _run([gpu, "---gpumpi", "-n", str(ranks), *GPU_OPTS], cwd=str(tmp_path / "gpu"))
     assert want.strip() and got == want
+    assert not list((tmp_path / "gpu").iterdir())
 
 
 # ---------------------------------------------------------------- the reference's programs
