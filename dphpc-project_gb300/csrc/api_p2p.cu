@@ -218,6 +218,20 @@ __device__ int MPI_Get_count(const MPI_Status* status, MPI_Datatype datatype, in
 }
 
 // ---------------------------------------------------------------- point to point
+// A blocking send or receive of an eager message on MPI_COMM_WORLD, with a
+// basic type, valid arguments and no posted receive or deferred send, takes
+// the leader-only path without a request object (p2p_send_small and
+// p2p_recv_small decide by size and buffer).  Anything else, and a full
+// mailbox, goes through the request path, which also reports argument errors.
+static __device__ __forceinline__ bool small_world_call(const BlockCtx& b, MPI_Comm comm, int count,
+                                                        MPI_Datatype datatype, u64* bytes) {
+    if (comm != &gm_world_sentinel || !b.p2p_quiet || count < 0 || (int)datatype < 0 ||
+        (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
+        return false;
+    *bytes = (u64)count * (u64)dtype_size(datatype);
+    return true;
+}
+
 static __device__ int start_send(const void* buf, int count, MPI_Datatype datatype, int dest,
                                  int tag, MPI_Comm comm, MPI_Request_impl** out) {
     API_ENTER();
@@ -355,6 +369,30 @@ __device__ int MPI_Isend(const void* buf, int count, MPI_Datatype datatype, int 
 
 __device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source, int tag,
                          MPI_Comm comm, MPI_Request* request) {
+    {
+        // a lazy receive: matched by the leader when it is waited for (lazy_progress)
+        BlockCtx& b = bctx();
+        u64 bytes;
+        if (small_world_call(b, comm, count, datatype, &bytes) && b.lazy_n < LAZY_MAX &&
+            (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
+            (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
+            if (api_abort_check(b)) return aborted_code();
+            MPI_Request_impl* r = req_alloc();
+            if (r) {
+                r->kind = RK_RECV;
+                r->peer = source;
+                r->tag = tag;
+                r->ctx = b.world_ctx;
+                r->bytes = bytes;
+                r->user_buf = buf;
+                r->buf = buf;
+                r->state = RS_LAZY;
+                b.lazy[b.lazy_n++] = r->index;
+                *request = r;
+                return MPI_SUCCESS;
+            }
+        }
+    }
     MPI_Request_impl* r = nullptr;
     int rc = start_recv(buf, count, datatype, source, tag, comm, &r);
     *request = r;
@@ -369,6 +407,10 @@ __device__ int MPI_Wait(MPI_Request* request, MPI_Status* status) {
     }
     MPI_Request_impl* r = *request;
     if (!req_valid(r)) return MPI_ERR_REQUEST;
+    if (r->state == RS_LAZY) {
+        const int rc = lazy_wait(r);   // done, or posted on the block path
+        if (rc) return rc;
+    }
     if (r->state != RS_DONE) {
         Call call;
         call.op = OP_WAIT;
@@ -389,6 +431,14 @@ __device__ int MPI_Test(MPI_Request* request, int* flag, MPI_Status* status) {
     }
     MPI_Request_impl* r = *request;
     if (!req_valid(r)) return MPI_ERR_REQUEST;
+    if (r->state == RS_LAZY) {
+        const int rc = lazy_progress();
+        if (rc) return rc;
+        if (r->state == RS_LAZY) {
+            *flag = 0;
+            return MPI_SUCCESS;
+        }
+    }
     int done = r->state == RS_DONE;
     if (!done) {
         Call call;
@@ -550,19 +600,6 @@ __device__ int MPI_Request_free(MPI_Request* request) {
     return rc;
 }
 
-// A blocking send or receive of an eager message on MPI_COMM_WORLD, with a
-// basic type, valid arguments and no posted receive or deferred send, takes
-// the leader-only path without a request object (p2p_send_small and
-// p2p_recv_small decide by size and buffer).  Anything else, and a full
-// mailbox, goes through the request path, which also reports argument errors.
-static __device__ __forceinline__ bool small_world_call(const BlockCtx& b, MPI_Comm comm, int count,
-                                                        MPI_Datatype datatype, u64* bytes) {
-    if (comm != &gm_world_sentinel || !b.p2p_quiet || count < 0 || (int)datatype < 0 ||
-        (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
-        return false;
-    *bytes = (u64)count * (u64)dtype_size(datatype);
-    return true;
-}
 
 __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag,
                         MPI_Comm comm) {
@@ -594,7 +631,7 @@ __device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source,
     {
         BlockCtx& b = bctx();
         u64 bytes;
-        if (small_world_call(b, comm, count, datatype, &bytes) &&
+        if (small_world_call(b, comm, count, datatype, &bytes) && b.lazy_n == 0 &&
             (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
             (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();

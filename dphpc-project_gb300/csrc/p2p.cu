@@ -564,9 +564,96 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int
     return 1;
 }
 
-// Leader: blocking receive of a small eager message on MPI_COMM_WORLD without
-// a request object.  The header's first 32 bytes are read as two vectors and,
-// for messages of up to 16 bytes, the payload with them.
+// ---------------------------------------------------------------- leader receives
+// A message of this rank's mailbox that matched (source, tag) on MPI_COMM_WORLD.
+struct SmallMatch {
+    int slot, src, tag, kind;
+    u64 bytes;
+    uint4 pre;   // the first 16 payload bytes of an eager message
+};
+
+// The oldest message among the `ready` slots matching (source, tag).  The
+// header's first 32 bytes are read as two vectors, the first 16 payload bytes
+// with them.
+static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, int source, int tag, SmallMatch* m) {
+    BlockCtx& b = bctx();
+    u64 best_stamp = ~0ull;
+    m->slot = -1;
+    while (ready) {
+        const int s = __ffsll((long long)ready) - 1;
+        ready &= ready - 1;
+        const int4 h0 = __ldcg((const int4*)&mb->hdr[s]);
+        const ulonglong2 h1 = __ldcg((const ulonglong2*)&mb->hdr[s].bytes);
+        const uint4 p0 = __ldcg((const uint4*)(slots + (u64)s * b.eager_bytes));
+        if (h0.x != b.world_ctx) continue;
+        if (source != MPI_ANY_SOURCE && h0.y != source) continue;
+        if (tag != MPI_ANY_TAG && h0.z != tag) continue;
+        if (h1.y < best_stamp) {
+            best_stamp = h1.y;
+            m->slot = s;
+            m->src = h0.y;
+            m->tag = h0.z;
+            m->kind = h0.w;
+            m->bytes = h1.x;
+            m->pre = p0;
+        }
+    }
+    return m->slot >= 0;
+}
+
+// Receive matched message m into buf (capacity `bytes`) and release its slot.
+// Returns 1 (done: *rc and *got set), or 0 when the request path must take it
+// (nothing consumed).
+static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatch& m, void* buf, u64 bytes,
+                                 int* rc, u64* got) {
+    BlockCtx& b = bctx();
+    const u64 n = m.bytes < bytes ? m.bytes : bytes;
+    const bool bulk = leader_bulk_ok(buf, n);
+    u32* rdv_done = nullptr;
+    const char* rdv_src = nullptr;
+    if (m.kind != 0) {
+        // rendezvous: the leader pulls from the sender's buffer when the bulk engine applies
+        const ulonglong2 h2 = __ldcg((const ulonglong2*)&mb->hdr[m.slot].rdv_src);
+        rdv_src = (const char*)h2.x;
+        rdv_done = (u32*)h2.y;
+        if (!bulk || ((uintptr_t)rdv_src & 15) != 0) return 0;
+    } else if (n > FAST_MSG_BYTES && !bulk) {
+        return 0;
+    }
+    char* d = (char*)buf;
+    *got = 0;
+    if (bulk) {
+        const u64 n16 = n & ~(u64)15;
+        const char* src = rdv_src ? rdv_src : slots + (u64)m.slot * b.eager_bytes;
+        *rc = leader_bulk_copy(d, src, n16);
+        if (*rc) return 1;   // the job has failed; the slot stays claimed
+        for (u64 i = n16; i < n; i++) d[i] = __ldcg(src + i);
+    } else if (n <= 16) {
+        const char* pc = (const char*)&m.pre;
+        for (u64 i = 0; i < n; i++) d[i] = pc[i];
+    } else {
+        const char* src = slots + (u64)m.slot * b.eager_bytes;
+        u64 i = 0;
+        if (((uintptr_t)d & 15) == 0) {
+            copy_vec16<true>((uint4*)d, (const uint4*)src, n >> 4);
+            i = n & ~(u64)15;
+        } else if (((uintptr_t)d & 7) == 0) {
+            for (; i + 8 <= n; i += 8) *(u64*)(d + i) = __ldcg((const u64*)(src + i));
+        }
+        for (; i < n; i++) d[i] = __ldcg(src + i);
+    }
+    red_and_relaxed(&mb->ready, ~(1ull << m.slot));
+    if (rdv_done) {
+        __threadfence();
+        st_release32(rdv_done, 1u);
+    }
+    red_and_release(&mb->used, ~(1ull << m.slot));
+    *rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
+    *got = n;
+    return 1;
+}
+
+// Leader: blocking receive on MPI_COMM_WORLD without a request object.
 __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc) {
     BlockCtx& b = bctx();
     Job* j = b.job;
@@ -576,82 +663,19 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
     unsigned ns = 32;
     for (;;) {
         // acquire on every poll: nothing read after it comes from L1 anyway
-        u64 ready = ld_acquire(&mb->ready);
-        if (ready) {
-            int best = -1;
-            u64 best_stamp = ~0ull, best_bytes = 0;
-            int best_src = 0, best_tag = 0, best_kind = 0;
-            uint4 pre = make_uint4(0, 0, 0, 0);
-            while (ready) {
-                const int s = __ffsll((long long)ready) - 1;
-                ready &= ready - 1;
-                const int4 h0 = __ldcg((const int4*)&mb->hdr[s]);
-                const ulonglong2 h1 = __ldcg((const ulonglong2*)&mb->hdr[s].bytes);
-                const uint4 p0 = __ldcg((const uint4*)(slots + (u64)s * b.eager_bytes));
-                if (h0.x != b.world_ctx) continue;
-                if (source != MPI_ANY_SOURCE && h0.y != source) continue;
-                if (tag != MPI_ANY_TAG && h0.z != tag) continue;
-                if (h1.y < best_stamp) {
-                    best_stamp = h1.y;
-                    best = s;
-                    best_src = h0.y;
-                    best_tag = h0.z;
-                    best_kind = h0.w;
-                    best_bytes = h1.x;
-                    pre = p0;
-                }
+        const u64 ready = ld_acquire(&mb->ready);
+        SmallMatch m;
+        if (ready && small_match(mb, slots, ready, source, tag, &m)) {
+            u64 got = 0;
+            if (!small_take(mb, slots, m, buf, bytes, rc, &got)) return 0;
+            if (st) {
+                st->MPI_SOURCE = m.src;
+                st->MPI_TAG = m.tag;
+                st->MPI_ERROR = *rc;
+                st->gpumpi_count_lo = (int)(got & 0xffffffffu);
+                st->gpumpi_count_hi = (int)(got >> 32);
             }
-            if (best >= 0) {
-                const u64 n = best_bytes < bytes ? best_bytes : bytes;
-                const bool bulk = leader_bulk_ok(buf, n);
-                u32* rdv_done = nullptr;
-                const char* rdv_src = nullptr;
-                if (best_kind != 0) {
-                    // rendezvous: the leader pulls from the sender's buffer when the bulk engine applies
-                    const ulonglong2 h2 = __ldcg((const ulonglong2*)&mb->hdr[best].rdv_src);
-                    rdv_src = (const char*)h2.x;
-                    rdv_done = (u32*)h2.y;
-                    if (!bulk || ((uintptr_t)rdv_src & 15) != 0) return 0;   // request path
-                } else if (n > FAST_MSG_BYTES && !bulk) {
-                    return 0;
-                }
-                char* d = (char*)buf;
-                if (bulk) {
-                    const u64 n16 = n & ~(u64)15;
-                    const char* src = rdv_src ? rdv_src : slots + (u64)best * b.eager_bytes;
-                    *rc = leader_bulk_copy(d, src, n16);
-                    if (*rc) return 1;   // the job has failed; the slot stays claimed
-                    for (u64 i = n16; i < n; i++) d[i] = __ldcg(src + i);
-                } else if (n <= 16) {
-                    const char* pc = (const char*)&pre;
-                    for (u64 i = 0; i < n; i++) d[i] = pc[i];
-                } else {
-                    const char* src = slots + (u64)best * b.eager_bytes;
-                    u64 i = 0;
-                    if (((uintptr_t)d & 15) == 0) {
-                        copy_vec16<true>((uint4*)d, (const uint4*)src, n >> 4);
-                        i = n & ~(u64)15;
-                    } else if (((uintptr_t)d & 7) == 0) {
-                        for (; i + 8 <= n; i += 8) *(u64*)(d + i) = __ldcg((const u64*)(src + i));
-                    }
-                    for (; i < n; i++) d[i] = __ldcg(src + i);
-                }
-                red_and_relaxed(&mb->ready, ~(1ull << best));
-                if (rdv_done) {
-                    __threadfence();
-                    st_release32(rdv_done, 1u);
-                }
-                red_and_release(&mb->used, ~(1ull << best));
-                *rc = best_bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
-                if (st) {
-                    st->MPI_SOURCE = best_src;
-                    st->MPI_TAG = best_tag;
-                    st->MPI_ERROR = *rc;
-                    st->gpumpi_count_lo = (int)(n & 0xffffffffu);
-                    st->gpumpi_count_hi = (int)(n >> 32);
-                }
-                return 1;
-            }
+            return 1;
         }
         if (ld_relaxed_int(&j->status[0]) != 0) {
             *rc = fail_code(j);
@@ -661,6 +685,104 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
             job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
             *rc = GPUMPI_ERR_TIMEOUT;
             return 1;
+        }
+        __nanosleep(ns);
+        if (ns < 128) ns <<= 1;
+    }
+}
+
+// ---------------------------------------------------------------- lazy receives
+// MPI_Irecv on MPI_COMM_WORLD while no receive is posted on the block path and
+// no send is deferred: the request waits in the block's FIFO of lazy receives
+// (posting order) instead of being posted.  A progress pass takes one snapshot
+// of the ready bits and lets every lazy receive, oldest first, take its oldest
+// matching message from that snapshot, so matching follows posting order, as
+// on the block path.  A message the leader cannot take (a rendezvous message
+// into a local buffer, ...), and every block-path call that matches messages,
+// first post all lazy receives on the block path, in order (lazy_materialize).
+
+// Post every lazy receive on the block path, oldest first.
+__device__ int lazy_materialize() {
+    BlockCtx& b = bctx();
+    const int n = b.lazy_n;
+    if (n == 0) return MPI_SUCCESS;
+    int idx[LAZY_MAX];
+    for (int i = 0; i < n; i++) idx[i] = b.lazy[i];
+    b.lazy_n = 0;
+    RankPriv* p = b.priv;
+    int first = MPI_SUCCESS;
+    for (int i = 0; i < n; i++) {
+        MPI_Request_impl* r = &p->reqs[idx[i]];
+        r->state = RS_NEW;
+        if (r->bytes && !is_global(r->buf)) {
+            void* g = heap_alloc(&b.job->heap, r->bytes);
+            if (!g) {
+                r->state = RS_DONE;
+                r->st_err = MPI_ERR_NO_MEM;
+                if (!first) first = MPI_ERR_NO_MEM;
+                continue;
+            }
+            r->buf = g;
+            r->stage_alloc = 1;
+        }
+        Call call;
+        call.op = OP_RECV_POST;
+        call.a[0] = (u64)r;
+        const int rc = block_call(call);
+        if (rc && !first) first = rc;
+    }
+    return first;
+}
+
+// One progress pass over the lazy receives.  Returns 0 or an error code.
+__device__ int lazy_progress() {
+    BlockCtx& b = bctx();
+    if (b.lazy_n == 0) return MPI_SUCCESS;
+    Mailbox* mb = &b.mbox[b.rank];
+    const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
+    u64 ready = ld_acquire(&mb->ready);
+    RankPriv* p = b.priv;
+    int i = 0;
+    while (i < b.lazy_n && ready) {
+        MPI_Request_impl* r = &p->reqs[b.lazy[i]];
+        SmallMatch m;
+        if (!small_match(mb, slots, ready, r->peer, r->tag, &m)) {
+            i++;
+            continue;
+        }
+        int rc = MPI_SUCCESS;
+        u64 got = 0;
+        if (!small_take(mb, slots, m, r->buf, r->bytes, &rc, &got)) return lazy_materialize();
+        ready &= ~(1ull << m.slot);
+        r->st_source = m.src;
+        r->st_tag = m.tag;
+        r->st_bytes = got;
+        r->st_err = rc;
+        r->state = RS_DONE;
+        for (int k = i + 1; k < b.lazy_n; k++) b.lazy[k - 1] = b.lazy[k];
+        b.lazy_n--;
+        if (rc && rc != MPI_ERR_TRUNCATE) return rc;
+    }
+    return MPI_SUCCESS;
+}
+
+// Leader: wait for lazy receive r.  On return r is done, or (after a
+// materialisation) posted on the block path; 0 or an error code.
+__device__ int lazy_wait(MPI_Request_impl* r) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    const u64 t0 = gtime();
+    unsigned ns = 32;
+    for (;;) {
+        const int rc = lazy_progress();
+        if (rc) return rc;
+        if (r->state != RS_LAZY) return MPI_SUCCESS;
+        // a deferred send needs the block path's progress: wait there
+        if (!b.p2p_quiet) return lazy_materialize();
+        if (ld_relaxed_int(&j->status[0]) != 0) return fail_code(j);
+        if (gtime() - t0 > b.timeout_ns) {
+            job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
+            return GPUMPI_ERR_TIMEOUT;
         }
         __nanosleep(ns);
         if (ns < 128) ns <<= 1;

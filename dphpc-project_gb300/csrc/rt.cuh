@@ -95,7 +95,8 @@ struct alignas(128) Mailbox {
 };
 
 enum ReqKind : int { RK_FREE = 0, RK_SEND = 1, RK_RECV = 2 };
-enum ReqState : int { RS_NEW = 0, RS_DEFERRED, RS_POSTED, RS_WAIT_RDV, RS_DONE };
+enum ReqState : int { RS_NEW = 0, RS_DEFERRED, RS_POSTED, RS_WAIT_RDV, RS_DONE, RS_LAZY };
+constexpr int LAZY_MAX = 16;   // receives an MPI_Irecv may leave unposted (see lazy_progress)
 
 }  // namespace gm
 
@@ -511,6 +512,8 @@ struct BlockCtx {
     int world_ctx, world_size;
     int p2p_quiet;                // no posted receive and no deferred send
     unsigned api_calls;           // counts calls between checks of the abort word
+    int lazy_n;                   // lazy receives (request indices), oldest first
+    int lazy[LAZY_MAX];
 };
 
 static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");
@@ -629,6 +632,9 @@ constexpr u64 SMALL_BULK_MIN = 512;    // leader copies from this size go throug
 __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
 __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
 __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc);
+__device__ int lazy_materialize();
+__device__ int lazy_progress();
+__device__ int lazy_wait(MPI_Request_impl* r);
 __device__ bool p2p_send_fast(MPI_Request_impl* r);
 __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled);
 __device__ int p2p_recv_post(MPI_Request_impl* r, int tid, int T);

@@ -303,6 +303,15 @@ __device__ void blk_memset(void* dst, int c, u64 n, int tid, int T) {
 // ---------------------------------------------------------------- call protocol
 __device__ int block_call(Call& c) {
     BlockCtx& b = bctx();
+    // Lazy receives go to the block path before any point-to-point call there:
+    // it matches in posting order, and a wait on a rendezvous send needs the
+    // receives it depends on to progress (two ranks in MPI_Sendrecv).
+    if (b.lazy_n > 0 &&
+        (c.op == OP_SEND_START || c.op == OP_RECV_POST || c.op == OP_WAIT || c.op == OP_TEST ||
+         c.op == OP_PROBE || c.op == OP_FINALIZE)) {
+        const int rc = lazy_materialize();
+        if (rc) return rc;
+    }
     b.call = c;
     b.in_call = 1;
     bar_named(1, b.T);
@@ -407,6 +416,7 @@ __device__ void rank_init(int tid, int T) {
         b.world_size = j->nranks;
         b.p2p_quiet = 1;
         b.api_calls = 0;
+        b.lazy_n = 0;
         w.rank = r;
         w.refcnt = 1;
         w.cs = j->world_cs;
@@ -471,6 +481,7 @@ __device__ bool program_block_begin(const Launch& L) {
             b.leader_mode = 1;
             b.in_call = 0;
             b.bulk_broken = 0;
+            b.lazy_n = 0;
             b.call.op = -1;
         }
     }
