@@ -264,6 +264,10 @@ static __device__ int start_send(const void* buf, int count, MPI_Datatype dataty
         *out = r;
         return MPI_SUCCESS;
     }
+    if (p2p_send_rdv_fast(r)) {   // rendezvous from a global buffer, nothing posted on the block path
+        *out = r;
+        return MPI_SUCCESS;
+    }
     if (bytes && !is_global(buf)) {
         void* g = heap_alloc(&b.job->heap, bytes);
         if (!g) {
@@ -409,6 +413,10 @@ __device__ int MPI_Wait(MPI_Request* request, MPI_Status* status) {
     if (!req_valid(r)) return MPI_ERR_REQUEST;
     if (r->state == RS_LAZY) {
         const int rc = lazy_wait(r);   // done, or posted on the block path
+        if (rc) return rc;
+    }
+    if (r->state == RS_WAIT_RDV && b.p2p_quiet) {
+        const int rc = rdv_wait_leader(r);   // done, or the block path takes over
         if (rc) return rc;
     }
     if (r->state != RS_DONE) {

@@ -433,17 +433,77 @@ static __device__ void leader_copy(void* dst, const void* src, u64 n) {
 }
 
 // Leader: send r (r->buf may be local memory) without the block.  False: use the block path.
+static __device__ int leader_bulk_copy(char* dst, const char* src, u64 n);
+static __device__ bool leader_bulk_ok(const void* p, u64 n);
+
 __device__ bool p2p_send_fast(MPI_Request_impl* r) {
     BlockCtx& b = bctx();
     Job* j = b.job;
-    if (r->bytes > FAST_MSG_BYTES || r->bytes > j->eager_bytes || b.priv->defer_head >= 0) return false;
+    // above FAST_MSG_BYTES only through the bulk engine (global, aligned buffer)
+    const bool bulk = r->bytes > FAST_MSG_BYTES && leader_bulk_ok(r->buf, r->bytes);
+    if ((r->bytes > FAST_MSG_BYTES && !bulk) || r->bytes > j->eager_bytes || b.priv->defer_head >= 0)
+        return false;
     r->done = 0;
     const int slot = claim_and_fill(j, r);
     if (slot < 0) return false;
-    if (r->bytes) leader_copy(eager_slot(j, r->peer_world, slot), r->buf, r->bytes);
+    char* dst = eager_slot(j, r->peer_world, slot);
+    if (bulk) {
+        const u64 n16 = r->bytes & ~(u64)15;
+        const int rc = leader_bulk_copy(dst, (const char*)r->buf, n16);
+        if (rc) {   // the job has failed; nothing is published
+            r->st_err = rc;
+            r->state = RS_DONE;
+            return true;
+        }
+        for (u64 i = n16; i < r->bytes; i++) dst[i] = ((const char*)r->buf)[i];
+    } else if (r->bytes) {
+        leader_copy(dst, r->buf, r->bytes);
+    }
     red_or_release(&j->mbox[r->peer_world].ready, 1ull << slot);
     r->state = RS_DONE;
     return true;
+}
+
+// Leader: nonblocking rendezvous send from a global buffer while nothing is
+// posted on the block path: the header points the receiver at r->buf and at
+// r->done; the request then waits for the receiver's pull (rdv_wait_leader).
+__device__ bool p2p_send_rdv_fast(MPI_Request_impl* r) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    if (r->bytes <= j->eager_bytes || !b.p2p_quiet || !is_global(r->buf)) return false;
+    r->done = 0;
+    const int slot = claim_and_fill(j, r);   // rendezvous header: rdv_src = r->buf, rdv_done = &r->done
+    if (slot < 0) return false;
+    red_or_release(&j->mbox[r->peer_world].ready, 1ull << slot);
+    r->state = RS_WAIT_RDV;
+    return true;
+}
+
+// Leader: wait until the receiver of rendezvous send r has pulled it, while
+// progressing this rank's lazy receives (the receiver may be waiting for a
+// rendezvous message of its own from this rank).  Returns 0 with r done, or 0
+// with r still waiting when the block path must take over, or an error code.
+__device__ int rdv_wait_leader(MPI_Request_impl* r) {
+    BlockCtx& b = bctx();
+    Job* j = b.job;
+    const u64 t0 = gtime();
+    unsigned ns = 32;
+    for (;;) {
+        if (ld_acquire32((const u32*)&r->done)) {
+            r->state = RS_DONE;
+            return MPI_SUCCESS;
+        }
+        const int rc = lazy_progress();
+        if (rc) return rc;
+        if (!b.p2p_quiet) return MPI_SUCCESS;   // block path receives posted: wait there
+        if (ld_relaxed_int(&j->status[0]) != 0) return fail_code(j);
+        if (gtime() - t0 > b.timeout_ns) {
+            job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
+            return GPUMPI_ERR_TIMEOUT;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+    }
 }
 
 // Leader: blocking send of a small eager message on MPI_COMM_WORLD, without a
@@ -460,7 +520,7 @@ static __device__ int leader_bulk_copy(char* dst, const char* src, u64 n) {
     return bp.finish();
 }
 
-static __device__ __forceinline__ bool leader_bulk_ok(const void* p, u64 n) {
+static __device__ bool leader_bulk_ok(const void* p, u64 n) {
     return n >= SMALL_BULK_MIN && ((uintptr_t)p & 15) == 0 && is_global(p) && !bctx().bulk_broken &&
            bulk_stage_bytes() >= 8192;
 }

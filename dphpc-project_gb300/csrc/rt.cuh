@@ -635,6 +635,8 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
 __device__ int lazy_materialize();
 __device__ int lazy_progress();
 __device__ int lazy_wait(MPI_Request_impl* r);
+__device__ bool p2p_send_rdv_fast(MPI_Request_impl* r);
+__device__ int rdv_wait_leader(MPI_Request_impl* r);
 __device__ bool p2p_send_fast(MPI_Request_impl* r);
 __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled);
 __device__ int p2p_recv_post(MPI_Request_impl* r, int tid, int T);
