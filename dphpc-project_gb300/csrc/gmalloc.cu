@@ -361,9 +361,20 @@ __device__ void heap_free(Heap* h, void* ptr) {
     const u32 cls = *(volatile u32*)&pm->cls;
     if (cls < NCLS) {
         const u64 chunk = (off % PAGE) >> (4 + cls);
+        const u32 word = (u32)(chunk / 64);
+        const u64 bit = 1ull << (chunk % 64);
+        // Lanes of a warp freeing chunks of the same bitmap word free them
+        // together: one fence and one atomicAnd for the group, by its lowest lane.
+        const unsigned act = __activemask();
+        const unsigned grp = __match_any_sync(act, ((unsigned long long)p << 8) | word);
+        const unsigned lo = __reduce_or_sync(grp, (unsigned)bit);
+        const unsigned hi = __reduce_or_sync(grp, (unsigned)(bit >> 32));
+        __syncwarp(grp);   // orders every lane's last use of its chunk before the leader's release
+        if ((int)(threadIdx.x & 31) != __ffs(grp) - 1) return;
+        // release: the group's chunks can be claimed again only after this
         __threadfence();
-        atomicAdd(&pm->nfree, 1u);
-        atomicAnd(&pm->bits[chunk / 64], ~(1ull << (chunk % 64)));
+        atomicAdd(&pm->nfree, (u32)__popc(grp));
+        atomicAnd(&pm->bits[word], ~(((u64)hi << 32) | lo));
         if (*(volatile u32*)&pm->listed == 0u) push_partial(h, (int)cls, p);
         return;
     }
