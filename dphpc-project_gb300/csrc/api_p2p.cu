@@ -218,16 +218,38 @@ __device__ int MPI_Get_count(const MPI_Status* status, MPI_Datatype datatype, in
 }
 
 // ---------------------------------------------------------------- point to point
-// A blocking send or receive of an eager message on MPI_COMM_WORLD, with a
-// basic type, valid arguments and no posted receive or deferred send, takes
-// the leader-only path without a request object (p2p_send_small and
-// p2p_recv_small decide by size and buffer).  Anything else, and a full
-// mailbox, goes through the request path, which also reports argument errors.
-static __device__ __forceinline__ bool small_world_call(const BlockCtx& b, MPI_Comm comm, int count,
-                                                        MPI_Datatype datatype, u64* bytes) {
-    if (comm != &gm_world_sentinel || !b.p2p_quiet || count < 0 || (int)datatype < 0 ||
-        (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
+// A blocking send or receive of an eager message with a basic type, valid
+// arguments and no posted receive or deferred send takes the leader-only path
+// without a request object (p2p_send_small and p2p_recv_small decide by size
+// and buffer).  Anything else, and a full mailbox, goes through the request
+// path, which also reports argument errors.
+
+// The communicator of a leader-path call: context, the caller's rank, size
+// and member table (nullptr: ranks are job ranks).  MPI_COMM_WORLD comes from
+// the block's cached fields without a memory read.
+struct SmallComm {
+    int ctx, me, size;
+    const int* members;
+    __device__ __forceinline__ int job_rank(int r) const { return members ? __ldcg(&members[r]) : r; }
+};
+
+static __device__ __forceinline__ bool small_call(const BlockCtx& b, MPI_Comm comm, int count,
+                                                  MPI_Datatype datatype, u64* bytes, SmallComm* sc) {
+    if (!b.p2p_quiet || count < 0 || (int)datatype < 0 || (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
         return false;
+    if (comm == &gm_world_sentinel) {
+        sc->ctx = b.world_ctx;
+        sc->me = b.rank;
+        sc->size = b.world_size;
+        sc->members = nullptr;
+    } else {
+        const MPI_Comm_impl* c = comm_resolve(comm);
+        if (!c) return false;
+        sc->ctx = c->ctx;
+        sc->me = c->rank;
+        sc->size = c->size;
+        sc->members = c->cs->members;
+    }
     *bytes = (u64)count * (u64)dtype_size(datatype);
     return true;
 }
@@ -377,8 +399,9 @@ __device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source
         // a lazy receive: matched by the leader when it is waited for (lazy_progress)
         BlockCtx& b = bctx();
         u64 bytes;
-        if (small_world_call(b, comm, count, datatype, &bytes) && b.lazy_n < LAZY_MAX &&
-            (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
+        SmallComm sc;
+        if (b.lazy_n < LAZY_MAX && small_call(b, comm, count, datatype, &bytes, &sc) &&
+            (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
             (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
             MPI_Request_impl* r = req_alloc();
@@ -386,7 +409,7 @@ __device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source
                 r->kind = RK_RECV;
                 r->peer = source;
                 r->tag = tag;
-                r->ctx = b.world_ctx;
+                r->ctx = sc.ctx;
                 r->bytes = bytes;
                 r->user_buf = buf;
                 r->buf = buf;
@@ -614,12 +637,16 @@ __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int d
     {
         BlockCtx& b = bctx();
         u64 bytes;
-        if (small_world_call(b, comm, count, datatype, &bytes) && dest >= 0 && dest < b.world_size &&
-            tag >= 0 && tag <= MPI_TAG_UB) {
+        SmallComm sc;
+        if (small_call(b, comm, count, datatype, &bytes, &sc) && dest >= 0 && dest < sc.size && tag >= 0 &&
+            tag <= MPI_TAG_UB) {
             if (api_abort_check(b)) return aborted_code();
             int rc = MPI_SUCCESS;
-            if (bytes <= b.eager_bytes ? p2p_send_small(buf, bytes, dest, tag, &rc)
-                                       : p2p_send_rdv_small(buf, bytes, dest, tag, &rc))
+            const int dj = sc.job_rank(dest);
+            // the blocking rendezvous waits without progressing lazy receives:
+            // with some pending, MPI_Wait on an MPI_Isend request waits instead
+            if (bytes <= b.eager_bytes ? p2p_send_small(buf, bytes, dj, sc.ctx, sc.me, tag, &rc)
+                                       : b.lazy_n == 0 && p2p_send_rdv_small(buf, bytes, dj, sc.ctx, sc.me, tag, &rc))
                 return rc;
         }
     }
@@ -639,12 +666,13 @@ __device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source,
     {
         BlockCtx& b = bctx();
         u64 bytes;
-        if (small_world_call(b, comm, count, datatype, &bytes) && b.lazy_n == 0 &&
-            (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
+        SmallComm sc;
+        if (b.lazy_n == 0 && small_call(b, comm, count, datatype, &bytes, &sc) &&
+            (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
             (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
             int rc = MPI_SUCCESS;
-            if (p2p_recv_small(buf, bytes, source, tag, status, &rc)) return rc;
+            if (p2p_recv_small(buf, bytes, sc.ctx, source, tag, status, &rc)) return rc;
         }
     }
     MPI_Request r = MPI_REQUEST_NULL;
@@ -661,15 +689,16 @@ __device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sen
         // An eager send completes without the receiver, so the leader may send
         // first and then receive (the halo exchanges of stencil codes).
         BlockCtx& b = bctx();
-        u64 sbytes, rbytes;
-        if (small_world_call(b, comm, sendcount, sendtype, &sbytes) && sbytes <= b.eager_bytes &&
-            small_world_call(b, comm, recvcount, recvtype, &rbytes) && dest >= 0 && dest < b.world_size &&
-            sendtag >= 0 && sendtag <= MPI_TAG_UB &&
-            (source == MPI_ANY_SOURCE || (source >= 0 && source < b.world_size)) &&
+        u64 sbytes;
+        SmallComm sc;
+        if (small_call(b, comm, sendcount, sendtype, &sbytes, &sc) && sbytes <= b.eager_bytes &&
+            recvcount >= 0 && (int)recvtype >= 0 && (int)recvtype < GPUMPI_NUM_BASIC_TYPES && dest >= 0 &&
+            dest < sc.size && sendtag >= 0 && sendtag <= MPI_TAG_UB &&
+            (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
             (recvtag == MPI_ANY_TAG || (recvtag >= 0 && recvtag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
             int rc = MPI_SUCCESS;
-            if (p2p_send_small(sendbuf, sbytes, dest, sendtag, &rc)) {
+            if (p2p_send_small(sendbuf, sbytes, sc.job_rank(dest), sc.ctx, sc.me, sendtag, &rc)) {
                 if (rc) return rc;
                 return MPI_Recv(recvbuf, recvcount, recvtype, source, recvtag, comm, status);
             }

@@ -169,6 +169,8 @@ size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, cha
         memset(&s, 0, sizeof(s));
         s.size = 1;
         s.ctx = 2;
+        s.self_member = r;
+        s.members = (int*)(base + o_scs + sizeof(CommShared) * (size_t)r + offsetof(CommShared, self_member));
         s.pub = (Pub*)(base + o_spub) + r;
         s.arrive = (u64*)(base + o_sarr) + 3 * (size_t)r;
         s.mid = s.arrive + 1;

@@ -506,10 +506,6 @@ __device__ int rdv_wait_leader(MPI_Request_impl* r) {
     }
 }
 
-// Leader: blocking send of a small eager message on MPI_COMM_WORLD, without a
-// request object.  Reads only the block's shared-memory copies of job state;
-// the stamp and the slot claim are in flight together.  Returns 0 (before
-// publishing anything) when the destination's mailbox is full.
 // The leader alone copies n bytes (a multiple of 16) between 16-byte aligned
 // global buffers through the bulk engine: one load and one store round trip,
 // whatever n.  Returns 0 or an error code (the job has then failed).
@@ -548,22 +544,22 @@ static __device__ int claim_slot_small(Mailbox* mb) {
     }
 }
 
-// Leader: blocking rendezvous send on MPI_COMM_WORLD without a request object.
+// Leader: blocking rendezvous send without a request object.
 // The header points the receiver at the user's (global) buffer and at the
 // rank's completion word; the call returns once the receiver has copied the
 // data and set that word.  Returns 0 (before publishing) when buf is not in
 // global memory or the mailbox is full.
-__device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest, int tag, int* rc) {
+__device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc) {
     BlockCtx& b = bctx();
     if (!is_global(buf)) return 0;
-    Mailbox* mb = &b.mbox[dest];
+    Mailbox* mb = &b.mbox[dest_job];
     const u64 stamp = atomicAdd(&mb->stamp, 1ull);
     u32* done = &b.priv->rdv_done_small;
     *done = 0u;
     const int s = claim_slot_small(mb);
     if (s < 0) return 0;
     MsgHdr* h = &mb->hdr[s];
-    *(int4*)h = make_int4(b.world_ctx, b.rank, tag, 1);   // kind = rendezvous
+    *(int4*)h = make_int4(ctx, me, tag, 1);   // kind = rendezvous
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
     *(ulonglong2*)&h->rdv_src = make_ulonglong2((u64)buf, (u64)done);
     red_or_release(&mb->ready, 1ull << s);
@@ -587,11 +583,15 @@ __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest, int tag,
     return 1;
 }
 
-__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc) {
+// Leader: blocking send of an eager message without a request object.  Reads
+// only the block's shared-memory copies of job state; the stamp and the slot
+// claim are in flight together.  Returns 0 (before publishing anything) when
+// the destination's mailbox is full.
+__device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc) {
     BlockCtx& b = bctx();
     const bool bulk = leader_bulk_ok(buf, bytes);
     if (bytes > FAST_MSG_BYTES && !bulk) return 0;
-    Mailbox* mb = &b.mbox[dest];
+    Mailbox* mb = &b.mbox[dest_job];
     const u64 stamp = atomicAdd(&mb->stamp, 1ull);   // a skipped stamp only leaves a gap
     // up to 64 aligned bytes are loaded now, while the atomics are in flight
     const bool pre = bytes <= 64 && ((uintptr_t)buf & 15) == 0;
@@ -604,9 +604,9 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int
     const int s = claim_slot_small(mb);
     if (s < 0) return 0;
     MsgHdr* h = &mb->hdr[s];
-    *(int4*)h = make_int4(b.world_ctx, b.rank, tag, 0);   // ctx, src, tag, kind = eager
+    *(int4*)h = make_int4(ctx, me, tag, 0);   // ctx, src, tag, kind = eager
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
-    char* slot = b.eager + ((u64)dest * MB_SLOTS + s) * b.eager_bytes;
+    char* slot = b.eager + ((u64)dest_job * MB_SLOTS + s) * b.eager_bytes;
     *rc = MPI_SUCCESS;
     if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
 #pragma unroll
@@ -625,17 +625,18 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int
 }
 
 // ---------------------------------------------------------------- leader receives
-// A message of this rank's mailbox that matched (source, tag) on MPI_COMM_WORLD.
+// A message of this rank's mailbox that matched (ctx, source, tag).
 struct SmallMatch {
     int slot, src, tag, kind;
     u64 bytes;
     uint4 pre;   // the first 16 payload bytes of an eager message
 };
 
-// The oldest message among the `ready` slots matching (source, tag).  The
+// The oldest message among the `ready` slots matching (ctx, source, tag).  The
 // header's first 32 bytes are read as two vectors, the first 16 payload bytes
 // with them.
-static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, int source, int tag, SmallMatch* m) {
+static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, int ctx, int source, int tag,
+                                   SmallMatch* m) {
     BlockCtx& b = bctx();
     u64 best_stamp = ~0ull;
     m->slot = -1;
@@ -645,7 +646,7 @@ static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, in
         const int4 h0 = __ldcg((const int4*)&mb->hdr[s]);
         const ulonglong2 h1 = __ldcg((const ulonglong2*)&mb->hdr[s].bytes);
         const uint4 p0 = __ldcg((const uint4*)(slots + (u64)s * b.eager_bytes));
-        if (h0.x != b.world_ctx) continue;
+        if (h0.x != ctx) continue;
         if (source != MPI_ANY_SOURCE && h0.y != source) continue;
         if (tag != MPI_ANY_TAG && h0.z != tag) continue;
         if (h1.y < best_stamp) {
@@ -713,8 +714,8 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
     return 1;
 }
 
-// Leader: blocking receive on MPI_COMM_WORLD without a request object.
-__device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc) {
+// Leader: blocking receive without a request object.
+__device__ int p2p_recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st, int* rc) {
     BlockCtx& b = bctx();
     Job* j = b.job;
     Mailbox* mb = &b.mbox[b.rank];
@@ -725,7 +726,7 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
         // acquire on every poll: nothing read after it comes from L1 anyway
         const u64 ready = ld_acquire(&mb->ready);
         SmallMatch m;
-        if (ready && small_match(mb, slots, ready, source, tag, &m)) {
+        if (ready && small_match(mb, slots, ready, ctx, source, tag, &m)) {
             u64 got = 0;
             if (!small_take(mb, slots, m, buf, bytes, rc, &got)) return 0;
             if (st) {
@@ -752,7 +753,7 @@ __device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Sta
 }
 
 // ---------------------------------------------------------------- lazy receives
-// MPI_Irecv on MPI_COMM_WORLD while no receive is posted on the block path and
+// MPI_Irecv while no receive is posted on the block path and
 // no send is deferred: the request waits in the block's FIFO of lazy receives
 // (posting order) instead of being posted.  A progress pass takes one snapshot
 // of the ready bits and lets every lazy receive, oldest first, take its oldest
@@ -806,7 +807,7 @@ __device__ int lazy_progress() {
     while (i < b.lazy_n && ready) {
         MPI_Request_impl* r = &p->reqs[b.lazy[i]];
         SmallMatch m;
-        if (!small_match(mb, slots, ready, r->peer, r->tag, &m)) {
+        if (!small_match(mb, slots, ready, r->ctx, r->peer, r->tag, &m)) {
             i++;
             continue;
         }
@@ -857,7 +858,8 @@ __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled) {
     Job* j = b.job;
     RankPriv* p = b.priv;
     *handled = 0;
-    if (p->recv_head >= 0 || p->defer_head >= 0) return MPI_SUCCESS;
+    // lazy receives were posted earlier and match first: the block path posts them, then r
+    if (p->recv_head >= 0 || p->defer_head >= 0 || b.lazy_n) return MPI_SUCCESS;
     Mailbox* mb = &j->mbox[b.rank];
     const u64 t0 = gtime();
     unsigned ns = 32;

@@ -164,6 +164,7 @@ struct alignas(128) CommShared {
     int topo_ndims;     // Cartesian topology (0 = none)
     int topo_dims[8];
     int topo_periods[8];
+    int self_member;    // a rank's MPI_COMM_SELF: members points here, at its job rank
 };
 
 }  // namespace gm
@@ -624,14 +625,16 @@ __device__ void fold_range(int opi, MPI_User_function* ufn, MPI_Datatype base, i
 __device__ int p2p_send_start(MPI_Request_impl* r, int tid, int T);
 constexpr u64 FAST_MSG_BYTES = 1024;   // eager messages the leader moves alone
 constexpr u64 SMALL_BULK_MIN = 512;    // leader copies from this size go through the bulk engine
-// Blocking send/receive of an eager message on MPI_COMM_WORLD by the leader,
-// without a request object: up to FAST_MSG_BYTES always, up to the eager size
-// when the user buffer is global, 16-byte aligned and the block has a bulk
-// staging area.  Return 1 when done (*rc set), 0 when the request path must
-// take the call.
-__device__ int p2p_send_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
-__device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest, int tag, int* rc);
-__device__ int p2p_recv_small(void* buf, u64 bytes, int source, int tag, MPI_Status* st, int* rc);
+// Blocking send/receive of an eager message by the leader, without a request
+// object: up to FAST_MSG_BYTES always, up to the eager size when the user
+// buffer is global, 16-byte aligned and the block has a bulk staging area.
+// ctx is the communicator's context, me the caller's rank in it (the source
+// the receiver matches), dest_job the destination's job rank and source a
+// rank of the communicator (or MPI_ANY_SOURCE).  Return 1 when done (*rc
+// set), 0 when the request path must take the call.
+__device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc);
+__device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc);
+__device__ int p2p_recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st, int* rc);
 __device__ int lazy_materialize();
 __device__ int lazy_progress();
 __device__ int lazy_wait(MPI_Request_impl* r);

@@ -342,6 +342,188 @@ __device__ int completion(int rank, int size) {
     return ok;
 }
 
+// MPI_COMM_SELF: messages to oneself (eager and rendezvous sizes), the member's
+// job rank through its group, a collective and a duplicate, with WORLD traffic
+// of the same tag in flight.
+__device__ int self_comm(int rank, int size) {
+    int ok = 1, me = -1, n = -1;
+    MPI_Comm_rank(MPI_COMM_SELF, &me);
+    MPI_Comm_size(MPI_COMM_SELF, &n);
+    if (me != 0 || n != 1) ok = 0;
+    const int next = (rank + 1) % size, prev = (rank + size - 1) % size;
+    int wx = 5000 + rank, wy = -1, x = 7000 + rank, y = -1;
+    MPI_Request rw[2], rs;
+    MPI_Irecv(&wy, 1, MPI_INT, prev, 5, MPI_COMM_WORLD, &rw[0]);
+    MPI_Isend(&wx, 1, MPI_INT, next, 5, MPI_COMM_WORLD, &rw[1]);
+    MPI_Isend(&x, 1, MPI_INT, 0, 5, MPI_COMM_SELF, &rs);
+    MPI_Status st;
+    MPI_Recv(&y, 1, MPI_INT, 0, 5, MPI_COMM_SELF, &st);
+    MPI_Wait(&rs, MPI_STATUS_IGNORE);
+    MPI_Waitall(2, rw, MPI_STATUSES_IGNORE);
+    if (y != 7000 + rank || st.MPI_SOURCE != 0 || st.MPI_TAG != 5) ok = 0;
+    if (wy != 5000 + prev) ok = 0;
+    const int big = 1 << 16;
+    int* a = (int*)malloc(sizeof(int) * big);
+    int* b = (int*)malloc(sizeof(int) * big);
+    for (int i = 0; i < big; i++) {
+        a[i] = rank * 131 + i;
+        b[i] = -1;
+    }
+    MPI_Sendrecv(a, big, MPI_INT, 0, 9, b, big, MPI_INT, 0, 9, MPI_COMM_SELF, &st);
+    for (int i = 0; i < big; i++)
+        if (b[i] != rank * 131 + i) {
+            ok = 0;
+            break;
+        }
+    MPI_Group gs, gw;
+    MPI_Comm_group(MPI_COMM_SELF, &gs);
+    MPI_Comm_group(MPI_COMM_WORLD, &gw);
+    int zero = 0, wr = -1;
+    MPI_Group_translate_ranks(gs, 1, &zero, gw, &wr);
+    if (wr != rank) ok = 0;
+    MPI_Group_free(&gs);
+    MPI_Group_free(&gw);
+    int sum = 0;
+    MPI_Allreduce(&x, &sum, 1, MPI_INT, MPI_SUM, MPI_COMM_SELF);
+    if (sum != x) ok = 0;
+    MPI_Comm d;
+    MPI_Comm_dup(MPI_COMM_SELF, &d);
+    int dx = 9000 + rank, dy = -1;
+    MPI_Sendrecv(&dx, 1, MPI_INT, 0, 1, &dy, 1, MPI_INT, 0, 1, d, MPI_STATUS_IGNORE);
+    if (dy != dx) ok = 0;
+    MPI_Comm_free(&d);
+    free(a);
+    free(b);
+    return ok;
+}
+
+// Point to point on communicators from MPI_Comm_split (even and odd world
+// ranks, reversed order): blocking sends and receives, Sendrecv, receives
+// posted before the matching sends, rendezvous sizes and MPI_ANY_SOURCE, with
+// WORLD messages of the same tags in flight.  Sources in statuses are ranks
+// of the sub-communicator.
+__device__ int split_p2p(int rank, int size) {
+    int ok = 1, me = -1, n = -1;
+    MPI_Comm sub;
+    MPI_Comm_split(MPI_COMM_WORLD, rank % 2, size - rank, &sub);
+    MPI_Comm_rank(sub, &me);
+    MPI_Comm_size(sub, &n);
+    const int next = (me + 1) % n, prev = (me + n - 1) % n;
+    // a WORLD message of tag 3 to the next world rank, received at the end
+    const int wnext = (rank + 1) % size, wprev = (rank + size - 1) % size;
+    int wv = 100 + rank, wr = -1;
+    MPI_Request wreq[2];
+    MPI_Irecv(&wr, 1, MPI_INT, wprev, 3, MPI_COMM_WORLD, &wreq[0]);
+    MPI_Isend(&wv, 1, MPI_INT, wnext, 3, MPI_COMM_WORLD, &wreq[1]);
+    // blocking ring on sub, tag 3: even members send first
+    int x = 1000 * (rank % 2) + me, y = -1;
+    MPI_Status st;
+    if (me % 2 == 0) {
+        MPI_Send(&x, 1, MPI_INT, next, 3, sub);
+        MPI_Recv(&y, 1, MPI_INT, prev, 3, sub, &st);
+    } else {
+        MPI_Recv(&y, 1, MPI_INT, prev, 3, sub, &st);
+        MPI_Send(&x, 1, MPI_INT, next, 3, sub);
+    }
+    if (y != 1000 * (rank % 2) + prev || st.MPI_SOURCE != prev || st.MPI_TAG != 3) ok = 0;
+    // Sendrecv of 40 doubles the other way
+    double d[40], e[40];
+    for (int i = 0; i < 40; i++) d[i] = rank * 0.5 + i;
+    MPI_Sendrecv(d, 40, MPI_DOUBLE, prev, 4, e, 40, MPI_DOUBLE, next, 4, sub, &st);
+    int wnext_sub = -1;
+    {
+        MPI_Group gs, gw;
+        MPI_Comm_group(sub, &gs);
+        MPI_Comm_group(MPI_COMM_WORLD, &gw);
+        MPI_Group_translate_ranks(gs, 1, &next, gw, &wnext_sub);
+        MPI_Group_free(&gs);
+        MPI_Group_free(&gw);
+    }
+    for (int i = 0; i < 40; i++)
+        if (e[i] != wnext_sub * 0.5 + i) ok = 0;
+    if (st.MPI_SOURCE != next) ok = 0;
+    // receives posted first, then the sends: 8 bytes and 256 KiB
+    const int big = 1 << 16;
+    int* a = (int*)malloc(sizeof(int) * big);
+    int* b = (int*)malloc(sizeof(int) * big);
+    for (int i = 0; i < big; i++) {
+        a[i] = rank * 7 + i;
+        b[i] = -1;
+    }
+    long long sv = 5000 + rank, rv = -1;
+    MPI_Request rq[2];
+    MPI_Irecv(&rv, 1, MPI_LONG_LONG, prev, 6, sub, &rq[0]);
+    MPI_Irecv(b, big, MPI_INT, next, 7, sub, &rq[1]);
+    MPI_Send(&sv, 1, MPI_LONG_LONG, next, 6, sub);
+    MPI_Send(a, big, MPI_INT, prev, 7, sub);
+    MPI_Waitall(2, rq, MPI_STATUSES_IGNORE);
+    int wprev_sub = -1;
+    {
+        MPI_Group gs, gw;
+        MPI_Comm_group(sub, &gs);
+        MPI_Comm_group(MPI_COMM_WORLD, &gw);
+        MPI_Group_translate_ranks(gs, 1, &prev, gw, &wprev_sub);
+        MPI_Group_free(&gs);
+        MPI_Group_free(&gw);
+    }
+    if (rv != 5000 + wprev_sub) ok = 0;
+    for (int i = 0; i < big; i++)
+        if (b[i] != wnext_sub * 7 + i) {
+            ok = 0;
+            break;
+        }
+    // member 0 gathers one value from every other member with MPI_ANY_SOURCE
+    if (me == 0) {
+        int seen = 0;
+        for (int k = 1; k < n; k++) {
+            int v = -1;
+            MPI_Recv(&v, 1, MPI_INT, MPI_ANY_SOURCE, 8, sub, &st);
+            if (st.MPI_SOURCE < 1 || st.MPI_SOURCE >= n || v != 300 + st.MPI_SOURCE) ok = 0;
+            seen |= 1 << st.MPI_SOURCE;
+        }
+        if (seen != ((1 << n) - 2)) ok = 0;
+    } else {
+        int v = 300 + me;
+        MPI_Send(&v, 1, MPI_INT, 0, 8, sub);
+    }
+    MPI_Waitall(2, wreq, MPI_STATUSES_IGNORE);
+    if (wr != 100 + wprev) ok = 0;
+    MPI_Comm_free(&sub);
+    free(a);
+    free(b);
+    return ok;
+}
+
+// Matching follows posting order: messages already in the mailbox go to the
+// earliest posted matching receive, whether it was posted by MPI_Irecv (still
+// waiting) or by a later blocking MPI_Recv.
+__device__ int posted_order(int rank, int size) {
+    int ok = 1;
+    if (rank == 1) {
+        for (int i = 0; i < 4; i++) {
+            int v = 10 + i;
+            MPI_Send(&v, 1, MPI_INT, 0, 5, MPI_COMM_WORLD);
+        }
+    }
+    MPI_Barrier(MPI_COMM_WORLD);   // the eager messages are in rank 0's mailbox
+    if (rank == 0) {
+        int a = -1, b = -1, c = -1, d = -1;
+        MPI_Request ra, rc;
+        MPI_Status st;
+        MPI_Irecv(&a, 1, MPI_INT, MPI_ANY_SOURCE, 5, MPI_COMM_WORLD, &ra);
+        MPI_Recv(&b, 1, MPI_INT, 1, 5, MPI_COMM_WORLD, &st);
+        MPI_Irecv(&c, 1, MPI_INT, 1, MPI_ANY_TAG, MPI_COMM_WORLD, &rc);
+        MPI_Sendrecv(&a, 0, MPI_INT, 0, 9, &d, 1, MPI_INT, 1, 5, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+        MPI_Wait(&rc, MPI_STATUS_IGNORE);
+        MPI_Wait(&ra, MPI_STATUS_IGNORE);
+        int z = -1;
+        MPI_Recv(&z, 0, MPI_INT, 0, 9, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+        ok = a == 10 && b == 11 && c == 12 && d == 13 && st.MPI_SOURCE == 1;
+    }
+    MPI_Barrier(MPI_COMM_WORLD);
+    return ok;
+}
+
 __device__ int __gpu_main(int argc, char** argv) {
     int rank, size, ok = 0;
     MPI_Init(&argc, &argv);
@@ -360,6 +542,9 @@ __device__ int __gpu_main(int argc, char** argv) {
     else if (!strcmp(s, "probe_order")) ok = probe_order(rank, size);
     else if (!strcmp(s, "large")) ok = large(rank, size);
     else if (!strcmp(s, "completion")) ok = completion(rank, size);
+    else if (!strcmp(s, "self_comm")) ok = self_comm(rank, size);
+    else if (!strcmp(s, "split_p2p")) ok = split_p2p(rank, size);
+    else if (!strcmp(s, "posted_order")) ok = posted_order(rank, size);
     printf("%s rank %d ok %d\n", s, rank, ok);
     MPI_Finalize();
     return 0;

@@ -17,6 +17,11 @@ KAT_CASES = [
     ("kat_p2p", "probe_order", 2),
     ("kat_p2p", "large", 4),
     ("kat_p2p", "completion", 4),
+    ("kat_p2p", "self_comm", 4),
+    ("kat_p2p", "split_p2p", 6),
+    ("kat_p2p", "split_p2p", 9),
+    ("kat_p2p", "posted_order", 2),
+    ("kat_p2p", "posted_order", 3),
     ("kat_coll", "reduce_prod", 5),
     ("kat_coll", "allreduce_sum", 7),
     ("kat_coll", "allgather", 7),
