@@ -117,14 +117,20 @@ class ClockSampler:
 NCU_TRAFFIC_BYTES_2_15 = 0.977500672e9 + 1.445693e9
 
 
-def alg_bytes(sizes, n):
+ALL_KINDS = ("bcast", "allreduce", "alltoall")
+
+
+def alg_bytes(sizes, n, kinds=ALL_KINDS):
     total = 0
     for p in sizes:
         for s in (4, 8):
-            total += p * n * s              # Bcast
-            total += 2 * p * n * s          # Allreduce
+            if "bcast" in kinds:
+                total += p * n * s              # Bcast
+            if "allreduce" in kinds:
+                total += 2 * p * n * s          # Allreduce
             per = n // p
-            total += 2 * p * p * per * s    # Alltoall
+            if "alltoall" in kinds:
+                total += 2 * p * p * per * s    # Alltoall
     return total
 
 
@@ -137,8 +143,9 @@ def max_over_ranks(dist, torch, secs: float) -> float:
     return float(t.item())
 
 
-def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1):
-    """Device buffers (one tensor per communicator and role) and descriptors."""
+def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1, kinds=ALL_KINDS):
+    """Device buffers (one tensor per communicator and role) and descriptors
+    of the collectives named in kinds."""
     g = torch.Generator(device="cuda").manual_seed(seed)
     dev = torch.device("cuda")
     comms, keep, descs, bufs = [], [], [], []
@@ -152,16 +159,21 @@ def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1):
                 if dt == "int32":
                     return torch.randint(-(1 << 20), 1 << 20, (count,), dtype=tdt, device=dev, generator=g)
                 return torch.rand(count, dtype=tdt, device=dev, generator=g) * 2 - 1
-            bc = rnd(p * n)
-            ar_in, ar_out = rnd(p * n), torch.empty(p * n, dtype=tdt, device=dev)
-            a2_in, a2_out = rnd(p * per * p), torch.empty(p * per * p, dtype=tdt, device=dev)
-            bufs += [bc, ar_in, ar_out, a2_in, a2_out]
             ptr = lambda t, stride: [t.data_ptr() + r * stride * es for r in range(p)]
-            descs.append(coll.make_desc(c, coll.COLL_BCAST, dt, n, None, ptr(bc, n), 0, 0, keep))
-            descs.append(coll.make_desc(c, coll.COLL_ALLREDUCE, dt, n, ptr(ar_in, n), ptr(ar_out, n),
-                                        coll.OP_SUM, 0, keep))
-            descs.append(coll.make_desc(c, coll.COLL_ALLTOALL, dt, per, ptr(a2_in, per * p),
-                                        ptr(a2_out, per * p), 0, 0, keep))
+            if "bcast" in kinds:
+                bc = rnd(p * n)
+                bufs.append(bc)
+                descs.append(coll.make_desc(c, coll.COLL_BCAST, dt, n, None, ptr(bc, n), 0, 0, keep))
+            if "allreduce" in kinds:
+                ar_in, ar_out = rnd(p * n), torch.empty(p * n, dtype=tdt, device=dev)
+                bufs += [ar_in, ar_out]
+                descs.append(coll.make_desc(c, coll.COLL_ALLREDUCE, dt, n, ptr(ar_in, n), ptr(ar_out, n),
+                                            coll.OP_SUM, 0, keep))
+            if "alltoall" in kinds:
+                a2_in, a2_out = rnd(p * per * p), torch.empty(p * per * p, dtype=tdt, device=dev)
+                bufs += [a2_in, a2_out]
+                descs.append(coll.make_desc(c, coll.COLL_ALLTOALL, dt, per, ptr(a2_in, per * p),
+                                            ptr(a2_out, per * p), 0, 0, keep))
     plan = coll.Plan(lib, descs, threads=threads, batched=batched)
     return plan, comms, keep, bufs, descs
 
@@ -238,6 +250,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="built-in schedules, --threads for every launch")
     ap.add_argument("--tune-reps", type=int, default=3)
+    ap.add_argument("--kinds", default=",".join(ALL_KINDS),
+                    help="collectives of the timed plan (a subset is a diagnostic run, not the workload)")
     ap.add_argument("--profile-launch", action="store_true",
                     help="bracket one batched launch after the warm-up with cudaProfilerStart/Stop "
                          "(for ncu --profile-from-start off)")
@@ -268,7 +282,8 @@ def main():
 
     # batched form, graph-captured; schedules and thread counts from the autotuner
     # (it times candidates on these buffers before the timed region)
-    plan, comms, keep, bufs, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, args.threads)
+    kinds = tuple(k for k in ALL_KINDS if k in args.kinds.split(","))
+    plan, comms, keep, bufs, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, args.threads, kinds=kinds)
     tuning = None
     plain_threads = plain_algos = None
     threads = args.threads
@@ -307,7 +322,7 @@ def main():
     if err:
         raise SystemExit(f"device error during benchmark: {err}")
     secs = max_over_ranks(dist, torch, secs)
-    nbytes = alg_bytes(COMM_SIZES, n)
+    nbytes = alg_bytes(COMM_SIZES, n, kinds)
     per_step = secs / args.steps
     value = nbytes * args.steps * world / secs / 1e9
     kernel_gbs = nbytes / per_step / 1e9
@@ -412,7 +427,9 @@ def main():
             "vs_baseline": None,
             "dtype": "int32+f64",
             "data": "synthetic (seeded uniform int32 [-2^20,2^20), fp64 [-1,1))",
-            "config": {"workload": WORKLOAD, "elements_per_rank": n, "comm_sizes": COMM_SIZES,
+            "config": {"workload": WORKLOAD if kinds == ALL_KINDS else
+                       "diagnostic subset of the batched collectives: " + "+".join(kinds),
+                       "elements_per_rank": n, "comm_sizes": COMM_SIZES,
                        "threads_per_rank": threads, "form": "batched, CUDA graph replay",
                        "tuning": tuning,
                        "l2": "inputs larger than L2 (each step touches ~%.0f GB)" % (nbytes / 1e9),
@@ -424,7 +441,7 @@ def main():
                       "batched_over_tuned_plain": round(value / world / plain_tuned_gbs, 2) if plain_tuned_gbs else None},
             "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind,
-                         "traffic": int(NCU_TRAFFIC_BYTES_2_15 * n / (1 << 15)),
+                         "traffic": int(NCU_TRAFFIC_BYTES_2_15 * n / (1 << 15)) if kinds == ALL_KINDS else None,
                          "traffic_note": "bytes per launch, ncu DRAM read+write at 2^15 elements per rank "
                                          "scaled by elements per rank",
                          "algorithmic_bytes": int(nbytes)},

@@ -367,6 +367,134 @@ static __device__ void fold_user(MPI_User_function* fn, MPI_Datatype dt, int es,
     }
 }
 
+// ---------------------------------------------------------------- bulk-staged push
+// The same fold with the inputs staged through shared memory: cp.async.bulk
+// loads one chunk of 16*T bytes (one vector per thread) of one input into a
+// ring of ns stages, each with a "full" mbarrier (completed by the load's
+// bytes) and an "empty" mbarrier (one arrival per thread once it has read its
+// vector).  Loads are issued in fold order (chunk by chunk, input rank by
+// input rank) by thread 0, which refills a stage one step after consuming it,
+// so up to ns - 1 loads are in flight whatever the registers allow.  Results
+// go to the outputs with ordinary stores once a chunk's last input is folded.
+// Every wait is bounded by the job's timeout; returns 0 or an error code.
+// 0 once the phase of `parity` has completed; 1 once the job has failed, 2
+// after the job's timeout.
+static __device__ __forceinline__ int mbar_wait(u32 bar, u32 parity, u64 t0, const Job* j) {
+    for (unsigned it = 0;; it++) {
+        u32 done = 0;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return 0;
+        if ((it & 15u) == 15u) {
+            if (ld_relaxed_int(&j->status[0]) != 0) return 1;
+            if (gtime() - t0 > j->timeout_ns) return 2;
+        }
+    }
+}
+
+// Thread 0: load chunk ic of input iq (nv vectors from element lo) into stage ist.
+static __device__ __forceinline__ void fold_bulk_issue(const char* src, u32 len, u32 dst_s, u32 full) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(len) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst_s), "l"(src), "r"(len), "r"(full) : "memory");
+}
+
+template <class T, class O>
+static __device__ __noinline__ int fold_push_bulk_t(const char* const* ptab, const char* const* otab, int nin, u64 lo,
+                                                    u64 nvec, int tid, int T_, char* ring, u64* bars, int ns) {
+    const u32 C = (u32)T_ * 16;
+    const u64 K = (nvec + T_ - 1) / T_ * (u64)nin;
+    const u64 off = lo * sizeof(T);
+    const u32 ring_s = (u32)__cvta_generic_to_shared(ring);
+    const u32 full_s = (u32)__cvta_generic_to_shared(bars);   // full[0..ns), then empty[0..ns)
+    const u32 empty_s = full_s + 8u * (u32)ns;
+    Job* j = bctx().job;
+    // issue side (thread 0): the next load's step, first vector, input rank and stage
+    u64 issued = 0, iv0 = 0;
+    int iq = 0, ist = 0;
+#define GM_FOLD_ISSUE()                                                                                \
+    do {                                                                                               \
+        const u64 nv_ = nvec - iv0 < (u64)T_ ? nvec - iv0 : (u64)T_;                                   \
+        fold_bulk_issue(ptab[iq] + off + iv0 * 16, (u32)(nv_ * 16), ring_s + (u32)ist * C,             \
+                        full_s + 8u * (u32)ist);                                                       \
+        issued++;                                                                                      \
+        if (++iq == nin) {                                                                             \
+            iq = 0;                                                                                    \
+            iv0 += (u64)T_;                                                                            \
+        }                                                                                              \
+        if (++ist == ns) ist = 0;                                                                      \
+    } while (0)
+    if (tid == 0)
+        while (issued < K && issued < (u64)ns) GM_FOLD_ISSUE();
+    int err = 0;
+    uint4 acc = make_uint4(0, 0, 0, 0);
+    const u64 t0 = gtime();
+    // consume side (every thread): this thread's vector, input rank, stage and phase
+    u64 v = (u64)tid;
+    int q = 0, st = 0, pst = ns - 1;
+    u32 par = 0, ppar = 1;
+    for (u64 k = 0; k < K; k++) {
+        err = mbar_wait(full_s + 8u * (u32)st, par, t0, j);
+        if (err) break;
+        if (v < nvec) {
+            const uint4 x = reinterpret_cast<const uint4*>(ring + st * C)[tid];
+            if (q == 0) acc = x;
+            else combine<T, O>(acc, x);
+        }
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(empty_s + 8u * (u32)st) : "memory");
+        if (tid == 0 && k >= 1 && issued < K) {
+            // refill the stage of step k - 1 once every thread has read it
+            err = mbar_wait(empty_s + 8u * (u32)pst, ppar, t0, j);
+            if (err) break;
+            GM_FOLD_ISSUE();
+        }
+        pst = st;
+        ppar = par;
+        if (++st == ns) {
+            st = 0;
+            par ^= 1u;
+        }
+        if (++q == nin) {
+            if (v < nvec)
+                for (int r = 0; r < nin; r++) reinterpret_cast<uint4*>(const_cast<char*>(otab[r]) + off)[v] = acc;
+            q = 0;
+            v += (u64)T_;
+        }
+    }
+#undef GM_FOLD_ISSUE
+    if (tid == 0 && err) {
+        // the loads still in flight write the ring: wait for them (bounded) before
+        // the block leaves; the caller keeps the block off the staging area
+        const u64 t1 = gtime();
+        const u64 first = issued > (u64)ns ? issued - (u64)ns : 0;
+        for (u64 k = first; k < issued; k++) {
+            const u32 bar = full_s + 8u * (u32)(k % (u64)ns);
+            const u32 p2 = (u32)((k / (u64)ns) & 1);
+            u32 done = 0;
+            while (!done && gtime() - t1 < j->timeout_ns)
+                asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                             : "=r"(done) : "r"(bar), "r"(p2) : "memory");
+        }
+    }
+    if (err == 2) job_fail(j, bctx().rank, GPUMPI_ERR_TIMEOUT, "bulk fold did not complete");
+    return err ? fail_code(j) : 0;
+}
+
+template <template <class> class O>
+static __device__ int fold_push_bulk_op(int canon, const char* const* ptab, const char* const* otab, int nin, u64 lo,
+                                        u64 nvec, int tid, int T_, char* ring, u64* bars, int ns) {
+    switch (canon) {
+        case K_I32: return fold_push_bulk_t<int, O<int>>(ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns);
+        case K_U32: return fold_push_bulk_t<unsigned, O<unsigned>>(ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns);
+        case K_I64: return fold_push_bulk_t<long long, O<long long>>(ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns);
+        case K_U64:
+            return fold_push_bulk_t<unsigned long long, O<unsigned long long>>(ptab, otab, nin, lo, nvec, tid, T_, ring,
+                                                                               bars, ns);
+        case K_F32: return fold_push_bulk_t<float, O<float>>(ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns);
+        default: return fold_push_bulk_t<double, O<double>>(ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns);
+    }
+}
+
 template <template <class> class O>
 static __device__ bool fold_push_op(int canon, const char* const* ptab, const char* const* otab, int nin, u64 lo,
                                     u64 hi, int tid, int T_) {
@@ -406,6 +534,53 @@ __device__ bool fold_range_push(int opi, MPI_Datatype base, const Pub* pub, int 
         bad |= ((((uintptr_t)ptab[q]) | ((uintptr_t)otab[q])) & 15) != 0;
     }
     if (bar_or(bad, T_)) return false;
+    // bulk staging: the ring and its 2 * ns mbarriers after the two tables
+    const u64 esz = basic_info((int)base).size;
+    const u64 nvec = hi > lo ? (hi - lo) * esz / 16 : 0;
+    const u32 tab_bytes = (u32)(2 * nin * sizeof(char*));
+    const u32 C = (u32)T_ * 16;
+    const u32 avail = bulk_stage_bytes();
+    int ns = 0;
+    if (!bctx().bulk_broken && nvec >= (u64)T_ && avail > tab_bytes + 256) {
+        ns = (int)((avail - tab_bytes - 256) / C);
+        if (ns > 16) ns = 16;
+    }
+    if (ns >= 4) {
+        u64* bars = reinterpret_cast<u64*>(gm_dsmem + BCTX_BYTES + BULK_BAR_BYTES + ((tab_bytes + 15) & ~15u));
+        char* ring = reinterpret_cast<char*>(bars) + 256;
+        if (tid < 2 * ns)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((u32)__cvta_generic_to_shared(&bars[tid])),
+                         "r"(tid < ns ? 1 : T_) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        bsync();
+        int rc = 0;
+        switch (opi) {
+            case 0: rc = fold_push_bulk_op<OMax>(canon, ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns); break;
+            case 1: rc = fold_push_bulk_op<OMin>(canon, ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns); break;
+            case 2: rc = fold_push_bulk_op<OSum>(canon, ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns); break;
+            default: rc = fold_push_bulk_op<OProd>(canon, ptab, otab, nin, lo, nvec, tid, T_, ring, bars, ns); break;
+        }
+        if (bar_or(rc != 0, T_)) {
+            bctx().bulk_broken = 1;   // loads may still be in flight into the ring
+            return true;              // the job has failed; peers leave their waits
+        }
+        if (tid < 2 * ns)
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"((u32)__cvta_generic_to_shared(&bars[tid])) : "memory");
+        // the elements after the last whole vector
+        const u64 done = nvec * 16 / esz;
+        if (lo + done < hi) {
+            switch (opi) {
+                case 0: fold_push_op<OMax>(canon, ptab, otab, nin, lo + done, hi, tid, T_); break;
+                case 1: fold_push_op<OMin>(canon, ptab, otab, nin, lo + done, hi, tid, T_); break;
+                case 2: fold_push_op<OSum>(canon, ptab, otab, nin, lo + done, hi, tid, T_); break;
+                default: fold_push_op<OProd>(canon, ptab, otab, nin, lo + done, hi, tid, T_); break;
+            }
+        }
+        bsync();
+        return true;
+    }
     if (hi > lo) {
         switch (opi) {
             case 0: fold_push_op<OMax>(canon, ptab, otab, nin, lo, hi, tid, T_); break;
