@@ -114,7 +114,7 @@ class ClockSampler:
 # DRAM bytes (read + write) of one batched launch at 2^15 elements per rank,
 # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); the
 # traffic grows in proportion with the per-rank count and is scaled by it.
-NCU_TRAFFIC_BYTES_2_15 = 0.977500672e9 + 1.445693e9
+NCU_TRAFFIC_BYTES_2_15 = 0.979630336e9 + 1.461430e9
 
 
 ALL_KINDS = ("bcast", "allreduce", "alltoall")
