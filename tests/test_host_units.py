@@ -63,3 +63,19 @@ def test_program_binaries_link_the_runtime(gpu_built):
     for p in progs:
         nm = subprocess.run(["nm", os.path.join(bindir, p)], capture_output=True, text=True)
         assert "gpumpi_main" in nm.stdout, p
+
+
+def test_bench_algorithmic_bytes_by_collective():
+    """The bench's byte counts: Bcast P*n*s, Allreduce 2*P*n*s, Alltoall 2*P^2*m
+    per communicator and type; a subset of collectives counts only its part."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    n = 1 << 10
+    sizes = bench.COMM_SIZES
+    per_type = sum(p * n for p in sizes) * (4 + 8)
+    assert bench.alg_bytes(sizes, n, ("bcast",)) == per_type
+    assert bench.alg_bytes(sizes, n, ("allreduce",)) == 2 * per_type
+    assert bench.alg_bytes(sizes, n, ("alltoall",)) == sum(2 * p * p * (n // p) for p in sizes) * (4 + 8)
+    assert bench.alg_bytes(sizes, n) == sum(bench.alg_bytes(sizes, n, (k,)) for k in bench.ALL_KINDS)
+    assert sum(sizes) == 1024 and len(sizes) == 16
