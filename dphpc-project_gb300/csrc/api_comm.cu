@@ -133,6 +133,7 @@ __device__ int MPI_Comm_free(MPI_Comm* comm) {
     RankPriv* p = bctx().priv;
     if (c != &p->comms[0] && c != &p->comms[1]) {
         if (--c->refcnt <= 0) c->kind = 0;
+        bctx().sc_handle = nullptr;   // the leader paths' cached communicator may be this one
     }
     *comm = MPI_COMM_NULL;
     return MPI_SUCCESS;

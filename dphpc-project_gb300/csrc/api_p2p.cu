@@ -226,7 +226,8 @@ __device__ int MPI_Get_count(const MPI_Status* status, MPI_Datatype datatype, in
 
 // The communicator of a leader-path call: context, the caller's rank, size
 // and member table (nullptr: ranks are job ranks).  MPI_COMM_WORLD comes from
-// the block's cached fields without a memory read.
+// the block's cached fields without a memory read, and so does the last other
+// communicator used (BlockCtx::sc_*, cleared by MPI_Comm_free).
 struct SmallComm {
     int ctx, me, size;
     const int* members;
@@ -242,6 +243,11 @@ static __device__ __forceinline__ bool small_call(const BlockCtx& b, MPI_Comm co
         sc->me = b.rank;
         sc->size = b.world_size;
         sc->members = nullptr;
+    } else if ((const void*)comm == b.sc_handle) {
+        sc->ctx = b.sc_ctx;
+        sc->me = b.sc_me;
+        sc->size = b.sc_size;
+        sc->members = b.sc_members;
     } else {
         const MPI_Comm_impl* c = comm_resolve(comm);
         if (!c) return false;
@@ -249,6 +255,12 @@ static __device__ __forceinline__ bool small_call(const BlockCtx& b, MPI_Comm co
         sc->me = c->rank;
         sc->size = c->size;
         sc->members = c->cs->members;
+        BlockCtx& w = const_cast<BlockCtx&>(b);
+        w.sc_handle = (const void*)comm;
+        w.sc_ctx = sc->ctx;
+        w.sc_me = sc->me;
+        w.sc_size = sc->size;
+        w.sc_members = sc->members;
     }
     *bytes = (u64)count * (u64)dtype_size(datatype);
     return true;

@@ -111,6 +111,7 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_plan_kernel(PlanArgs A
         b.in_call = 0;
         b.bulk_broken = 0;
         b.lazy_n = 0;
+        b.sc_handle = nullptr;
     }
     __syncthreads();
     MPI_Comm_impl* comm = &A.comms[c].handles[rank];

@@ -515,6 +515,12 @@ struct BlockCtx {
     unsigned api_calls;           // counts calls between checks of the abort word
     int lazy_n;                   // lazy receives (request indices), oldest first
     int lazy[LAZY_MAX];
+    // the last communicator other than MPI_COMM_WORLD resolved by a leader-path
+    // call (cleared when a communicator is freed): handle, context, the
+    // caller's rank, size and member table
+    const void* sc_handle;
+    const int* sc_members;
+    int sc_ctx, sc_me, sc_size;
 };
 
 static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");

@@ -417,6 +417,7 @@ __device__ void rank_init(int tid, int T) {
         b.p2p_quiet = 1;
         b.api_calls = 0;
         b.lazy_n = 0;
+        b.sc_handle = nullptr;
         w.rank = r;
         w.refcnt = 1;
         w.cs = j->world_cs;

@@ -11,8 +11,10 @@
 // every receive, the whole payload after the last one.  Rank 0 prints, per
 // size, the error count and a checksum of every received byte (equal between
 // a GPU run and a host MPI run), then on a separate line the time of the
-// slowest rank and the algorithmic bandwidth (2b per message).
-// Usage: p2p_sweep pairs|ring block|nb lg_min lg_max iters ---gpumpi -n P
+// slowest rank and the algorithmic bandwidth (2b per message).  With "dup"
+// the exchanges run on a duplicate of MPI_COMM_WORLD (same ranks, its own
+// context) instead of MPI_COMM_WORLD itself.
+// Usage: p2p_sweep pairs|ring block|nb lg_min lg_max iters [world|dup] ---gpumpi -n P
 #include "global_vars.cuh"
 #include "mpi.h.cuh"
 #include "stdio.h.cuh"
@@ -35,7 +37,7 @@ __device__ unsigned long long stamp_of(int rank, int it) {
 }
 
 __device__ int exchange(int pattern, int mode, int rank, int size, void* sbuf, void* rbuf, long b,
-                        int* src_out) {
+                        int* src_out, MPI_Comm comm) {
     int dst, src;
     if (pattern == 0) {
         dst = rank ^ 1;
@@ -52,16 +54,16 @@ __device__ int exchange(int pattern, int mode, int rank, int size, void* sbuf, v
     int rc = 0;
     if (mode == 0) {
         if ((rank & 1) == 0) {
-            rc |= MPI_Send(sbuf, (int)b, MPI_BYTE, dst, 7, MPI_COMM_WORLD);
-            rc |= MPI_Recv(rbuf, (int)b, MPI_BYTE, src, 7, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
+            rc |= MPI_Send(sbuf, (int)b, MPI_BYTE, dst, 7, comm);
+            rc |= MPI_Recv(rbuf, (int)b, MPI_BYTE, src, 7, comm, MPI_STATUS_IGNORE);
         } else {
-            rc |= MPI_Recv(rbuf, (int)b, MPI_BYTE, src, 7, MPI_COMM_WORLD, MPI_STATUS_IGNORE);
-            rc |= MPI_Send(sbuf, (int)b, MPI_BYTE, dst, 7, MPI_COMM_WORLD);
+            rc |= MPI_Recv(rbuf, (int)b, MPI_BYTE, src, 7, comm, MPI_STATUS_IGNORE);
+            rc |= MPI_Send(sbuf, (int)b, MPI_BYTE, dst, 7, comm);
         }
     } else {
         MPI_Request req[2];
-        rc |= MPI_Irecv(rbuf, (int)b, MPI_BYTE, src, 7, MPI_COMM_WORLD, &req[0]);
-        rc |= MPI_Isend(sbuf, (int)b, MPI_BYTE, dst, 7, MPI_COMM_WORLD, &req[1]);
+        rc |= MPI_Irecv(rbuf, (int)b, MPI_BYTE, src, 7, comm, &req[0]);
+        rc |= MPI_Isend(sbuf, (int)b, MPI_BYTE, dst, 7, comm, &req[1]);
         rc |= MPI_Waitall(2, req, MPI_STATUSES_IGNORE);
     }
     return rc;
@@ -73,7 +75,7 @@ __device__ int __gpu_main(int argc, char** argv) {
     MPI_Comm_rank(MPI_COMM_WORLD, &rank);
     MPI_Comm_size(MPI_COMM_WORLD, &size);
     if (argc < 6 || size < 2) {
-        if (rank == 0) printf("usage: p2p_sweep pairs|ring block|nb lg_min lg_max iters (2+ ranks)\n");
+        if (rank == 0) printf("usage: p2p_sweep pairs|ring block|nb lg_min lg_max iters [world|dup] (2+ ranks)\n");
         MPI_Finalize();
         return 1;
     }
@@ -82,6 +84,8 @@ __device__ int __gpu_main(int argc, char** argv) {
     const int lg_min = atoi(argv[3]) < 3 ? 3 : atoi(argv[3]);
     const int lg_max = atoi(argv[4]);
     const int iters = atoi(argv[5]) < 1 ? 1 : atoi(argv[5]);
+    MPI_Comm comm = MPI_COMM_WORLD;
+    if (argc > 6 && strcmp(argv[6], "dup") == 0) MPI_Comm_dup(MPI_COMM_WORLD, &comm);
     int status = 0;
     for (int lg = lg_min; lg <= lg_max; lg++) {
         const long b = 1L << lg;
@@ -106,7 +110,7 @@ __device__ int __gpu_main(int argc, char** argv) {
         int src = -1;
         for (int it = 0; it < iters; it++) {
             sbuf[0] = stamp_of(rank, it);
-            if (exchange(pattern, mode, rank, size, sbuf, rbuf, b, &src) != MPI_SUCCESS) errors++;
+            if (exchange(pattern, mode, rank, size, sbuf, rbuf, b, &src, comm) != MPI_SUCCESS) errors++;
             if (src >= 0 && rbuf[0] != stamp_of(src, it)) errors++;
         }
         double t1 = MPI_Wtime();
@@ -136,6 +140,7 @@ __device__ int __gpu_main(int argc, char** argv) {
         free(sbuf);
         free(rbuf);
     }
+    if (comm != MPI_COMM_WORLD) MPI_Comm_free(&comm);
     MPI_Finalize();
     return status;
 }

@@ -36,20 +36,23 @@ def test_gpu_coll_bench_matches_oracle(gpu_built, lg, iters, ranks):
 
 
 P2P_CASES = [
-    ("pairs", "block", 3, 16, 10, 2, "1G"),
-    ("ring", "block", 3, 14, 10, 7, "1G"),
-    ("pairs", "nb", 3, 20, 5, 64, "1G"),
-    ("ring", "nb", 10, 22, 3, 256, "4G"),
-    ("ring", "block", 3, 12, 4, 1024, "1G"),
-    ("pairs", "nb", 24, 26, 2, 8, "2G"),
+    ("pairs", "block", 3, 16, 10, 2, "1G", "world"),
+    ("ring", "block", 3, 14, 10, 7, "1G", "world"),
+    ("pairs", "nb", 3, 20, 5, 64, "1G", "world"),
+    ("ring", "nb", 10, 22, 3, 256, "4G", "world"),
+    ("ring", "block", 3, 12, 4, 1024, "1G", "world"),
+    ("pairs", "nb", 24, 26, 2, 8, "2G", "world"),
+    ("pairs", "block", 3, 20, 6, 4, "1G", "dup"),
+    ("ring", "nb", 3, 18, 4, 33, "1G", "dup"),
 ]
 
 
-@pytest.mark.parametrize("pattern,mode,lo,hi,iters,ranks,heap", P2P_CASES)
-def test_gpu_p2p_sweep_matches_oracle(gpu_built, pattern, mode, lo, hi, iters, ranks, heap):
+@pytest.mark.parametrize("pattern,mode,lo,hi,iters,ranks,heap,comm", P2P_CASES)
+def test_gpu_p2p_sweep_matches_oracle(gpu_built, pattern, mode, lo, hi, iters, ranks, heap, comm):
     """Point-to-point sweep: every payload arrives intact (errors 0) and the
-    per-size checksums of the received bytes equal the host MPI run's."""
-    args = [pattern, mode, str(lo), str(hi), str(iters)]
+    per-size checksums of the received bytes equal the host MPI run's, on
+    MPI_COMM_WORLD and on a duplicate of it."""
+    args = [pattern, mode, str(lo), str(hi), str(iters), comm]
     g = gpu_built.run_program("p2p_sweep", args, nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=300)
     c = gpu_built.run_oracle("p2p_sweep", args, nranks=ranks, timeout=300)
     assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
