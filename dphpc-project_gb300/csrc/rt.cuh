@@ -529,7 +529,7 @@ static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank s
 // gave more) the bulk-copy area: mbarriers, then staging buffers.
 constexpr int BCTX_BYTES = (int)((sizeof(BlockCtx) + 127) / 128 * 128);
 constexpr int BULK_BAR_BYTES = 128;
-constexpr int BULK_STAGES = 4;
+constexpr int BULK_STAGES = 3;
 constexpr u64 BULK_MIN_BYTES = 16 * 1024;   // blk_copy: smaller copies use vector loads
 constexpr u64 BULK_SEG_MIN = 4 * 1024;      // multi-segment copies: average segment size for the bulk engine
 __host__ __device__ constexpr size_t rank_smem_bytes(size_t stage) {
