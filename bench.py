@@ -144,39 +144,109 @@ def max_over_ranks(dist, torch, secs: float) -> float:
     return float(t.item())
 
 
+class Item:
+    """One collective call of the workload: its communicator size, type and
+    device buffers (send: the input of rank 0..P-1 back to back, recv: the
+    outputs; Bcast works in place on `recv`)."""
+
+    def __init__(self, kind, p, dt, count, send, recv):
+        self.kind, self.p, self.dt, self.count, self.send, self.recv = kind, p, dt, count, send, recv
+
+
+def fill_random(torch, t, dt, g):
+    if dt == "int32":
+        t.random_(-(1 << 20), 1 << 20, generator=g)
+    else:
+        t.uniform_(-1.0, 1.0, generator=g)
+
+
 def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1, kinds=ALL_KINDS):
-    """Device buffers (one tensor per communicator and role) and descriptors
-    of the collectives named in kinds."""
+    """Device buffers and descriptors of the collectives named in kinds, one
+    Item per descriptor (same order)."""
     g = torch.Generator(device="cuda").manual_seed(seed)
     dev = torch.device("cuda")
-    comms, keep, descs, bufs = [], [], [], []
+    comms, keep, descs, items = [], [], [], []
     for p in sizes:
         c = coll.Comm(lib, p)
         comms.append(c)
         per = n // p
         for dt, tdt in (("int32", torch.int32), ("float64", torch.float64)):
             es = 4 if dt == "int32" else 8
+
             def rnd(count):
-                if dt == "int32":
-                    return torch.randint(-(1 << 20), 1 << 20, (count,), dtype=tdt, device=dev, generator=g)
-                return torch.rand(count, dtype=tdt, device=dev, generator=g) * 2 - 1
+                t = torch.empty(count, dtype=tdt, device=dev)
+                fill_random(torch, t, dt, g)
+                return t
+
             ptr = lambda t, stride: [t.data_ptr() + r * stride * es for r in range(p)]
             if "bcast" in kinds:
                 bc = rnd(p * n)
-                bufs.append(bc)
+                items.append(Item("bcast", p, dt, n, None, bc))
                 descs.append(coll.make_desc(c, coll.COLL_BCAST, dt, n, None, ptr(bc, n), 0, 0, keep))
             if "allreduce" in kinds:
                 ar_in, ar_out = rnd(p * n), torch.empty(p * n, dtype=tdt, device=dev)
-                bufs += [ar_in, ar_out]
+                items.append(Item("allreduce", p, dt, n, ar_in, ar_out))
                 descs.append(coll.make_desc(c, coll.COLL_ALLREDUCE, dt, n, ptr(ar_in, n), ptr(ar_out, n),
                                             coll.OP_SUM, 0, keep))
             if "alltoall" in kinds:
                 a2_in, a2_out = rnd(p * per * p), torch.empty(p * per * p, dtype=tdt, device=dev)
-                bufs += [a2_in, a2_out]
+                items.append(Item("alltoall", p, dt, per, a2_in, a2_out))
                 descs.append(coll.make_desc(c, coll.COLL_ALLTOALL, dt, per, ptr(a2_in, per * p),
                                             ptr(a2_out, per * p), 0, 0, keep))
     plan = coll.Plan(lib, descs, threads=threads, batched=batched)
-    return plan, comms, keep, bufs, descs
+    return plan, comms, keep, items, descs
+
+
+def _bits(torch, t):
+    return t.view(torch.int64) if t.dtype == torch.float64 else t
+
+
+def verify_items(torch, items, sample: int | None = None, seed: int = 5) -> list[str]:
+    """Check every call's result against its inputs, bit for bit.
+
+    Bcast: every rank's buffer equals the root's (rank 0).  Alltoall: block q
+    of rank r's output equals block r of rank q's input.  Allreduce(SUM): the
+    output of every rank equals the rank-order fold acc = x_0; acc = x_q + acc
+    (q = 1..P-1) computed with NumPy on the host, the order of the reference's
+    MPI_Reduce (gpu_libs/gpu_mpi/mpi.cu:209-225); with `sample`, at that many
+    random element positions plus the first and last element of every rank's
+    segment, else at every element.  Returns the mismatches found."""
+    import numpy as np
+
+    bad = []
+    rng = np.random.default_rng(seed)
+    for k, it in enumerate(items):
+        p, n = it.p, it.count
+        if it.kind == "bcast":
+            m = _bits(torch, it.recv).view(p, n)
+            if not bool((m == m[0:1]).all()):
+                bad.append(f"item {k}: bcast P={p} {it.dt}")
+        elif it.kind == "alltoall":
+            per = n
+            src = _bits(torch, it.send).view(p, p, per)
+            dst = _bits(torch, it.recv).view(p, p, per)
+            if not torch.equal(dst, src.transpose(0, 1)):
+                bad.append(f"item {k}: alltoall P={p} {it.dt}")
+        elif it.kind == "allreduce":
+            x = it.send.view(p, n)
+            y = it.recv.view(p, n)
+            if sample is not None and sample < n:
+                seg = -(-n // p)
+                edges = [i for r in range(p) for i in (r * seg, min(n, (r + 1) * seg) - 1) if 0 <= i < n]
+                idx = np.unique(np.concatenate([rng.integers(0, n, sample), np.array(edges, dtype=np.int64)]))
+                ti = torch.from_numpy(idx).to(x.device)
+                xs = x.index_select(1, ti).cpu().numpy()
+                ys = y.index_select(1, ti).cpu().numpy()
+            else:
+                xs = x.cpu().numpy()
+                ys = y.cpu().numpy()
+            acc = xs[0].copy()
+            for q in range(1, p):
+                acc = xs[q] + acc
+            u = np.uint64 if acc.dtype.itemsize == 8 else np.uint32
+            if not bool((ys.view(u) == acc.view(u)[None, :]).all()):
+                bad.append(f"item {k}: allreduce P={p} {it.dt}")
+    return bad
 
 
 def time_plan(torch, plan, steps, warmup, stream):
@@ -251,6 +321,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="built-in schedules, --threads for every launch")
     ap.add_argument("--tune-reps", type=int, default=3)
+    ap.add_argument("--verify-sample", type=int, default=4096,
+                    help="element positions per Allreduce checked after the timed region")
     ap.add_argument("--kinds", default=",".join(ALL_KINDS),
                     help="collectives of the timed plan (a subset is a diagnostic run, not the workload)")
     ap.add_argument("--profile-launch", action="store_true",
@@ -284,7 +356,7 @@ def main():
     # batched form, graph-captured; schedules and thread counts from the autotuner
     # (it times candidates on these buffers before the timed region)
     kinds = tuple(k for k in ALL_KINDS if k in args.kinds.split(","))
-    plan, comms, keep, bufs, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, args.threads, kinds=kinds)
+    plan, comms, keep, items, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, args.threads, kinds=kinds)
     tuning = None
     plain_threads = plain_algos = None
     threads = args.threads
@@ -301,6 +373,12 @@ def main():
         tuning = {"batched_threads": threads, "algo_counts": algos, "seconds": round(tune_s, 2),
                   "plain_threads_counts": {str(t): plain_threads.count(t) for t in sorted(set(plain_threads))}}
         plan = coll.Plan(lib, descs, threads=threads, batched=True)
+        # the tuner ran the calls on these buffers: give every input (and the
+        # broadcast buffers of the non-root ranks) fresh data, so that the
+        # results checked after the timed region come from the timed launches
+        g = torch.Generator(device="cuda").manual_seed(11)
+        for it in items:
+            fill_random(torch, it.send if it.send is not None else it.recv, it.dt, g)
     plan.capture(stream.cuda_stream)
     launches0 = lib.gpumpi_kernel_launches()
     with torch.cuda.stream(stream):
@@ -323,6 +401,13 @@ def main():
     if err:
         raise SystemExit(f"device error during benchmark: {err}")
     secs = max_over_ranks(dist, torch, secs)
+    # outside the timed region: every call's result against its inputs, bit
+    # for bit (reductions at sampled element positions of every rank)
+    t0 = time.perf_counter()
+    bad = verify_items(torch, items, sample=args.verify_sample)
+    verify_s = time.perf_counter() - t0
+    if bad:
+        raise SystemExit("result mismatch after the timed region: " + "; ".join(bad[:8]))
     nbytes = alg_bytes(COMM_SIZES, n, kinds)
     per_step = secs / args.steps
     value = nbytes * args.steps * world / secs / 1e9
@@ -346,7 +431,7 @@ def main():
         plain_tuned_gbs = nbytes * args.plain_steps / psecs / 1e9
         plain.close()
     plan.close()
-    del bufs
+    del items
     torch.cuda.empty_cache()
 
     # end to end through the host-buffer entry point (smaller per-rank count).
@@ -357,7 +442,7 @@ def main():
     ne = 1 << args.e2e_lg
     ecomms, eplans, eparts = [], [], []
     for gi, group in enumerate(E2E_GROUPS):
-        eplan, gcomms, gkeep, gbufs, gdescs = build_plan(coll, lib, torch, group, ne, True, threads, seed=2 + gi)
+        eplan, gcomms, gkeep, gitems, gdescs = build_plan(coll, lib, torch, group, ne, True, threads, seed=2 + gi)
         ecomms += gcomms
         sizes_by_comm = {c.h.value: c.n for c in gcomms}
         layout = []
@@ -376,7 +461,7 @@ def main():
             hr.append(hrecv.data_ptr() + off)
             off += nb
         eplans.append(eplan)
-        eparts.append((eplan, hs, hr, torch.cuda.Stream(), (gkeep, gbufs, hsend, hrecv)))
+        eparts.append((eplan, hs, hr, torch.cuda.Stream(), (gkeep, gitems, hsend, hrecv)))
     ebytes = alg_bytes(COMM_SIZES, ne)
 
     def e2e_step():
@@ -452,6 +537,12 @@ def main():
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne,
                     "form": "gpumpi_plan_run_host, the 16 communicators as 4 batched plans on 4 streams"},
+            "verified": True,
+            "verification": {"what": "every call of the timed plan after the timed region: Bcast and Alltoall "
+                                     "outputs compared with their sources in full, Allreduce outputs of every "
+                                     "rank with a NumPy rank-order fold at %d sampled positions plus every "
+                                     "segment edge; bitwise" % args.verify_sample,
+                             "seconds": round(verify_s, 2)},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": int(launches),

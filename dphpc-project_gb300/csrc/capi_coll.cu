@@ -701,29 +701,36 @@ struct NoallocLayout {
     size_t job, status, err, cs, pub, flags, handles, dcomm, desc, first, ptrs, total;
 };
 
-NoallocLayout noalloc_layout(int n) {
-    NoallocLayout L;
+constexpr size_t noalloc_take(size_t& o, size_t bytes) {
+    o = (o + 255) & ~(size_t)255;
+    const size_t at = o;
+    o += bytes;
+    return at;
+}
+
+constexpr NoallocLayout noalloc_layout(int n) {
+    NoallocLayout L{};
     size_t o = 0;
-    auto take = [&](size_t bytes) {
-        o = (o + 255) & ~(size_t)255;
-        size_t at = o;
-        o += bytes;
-        return at;
-    };
-    L.job = take(sizeof(Job));
-    L.status = take(sizeof(int) * 16);
-    L.err = take(256);
-    L.cs = take(sizeof(CommShared));
-    L.pub = take(sizeof(Pub) * n);
-    L.flags = take(sizeof(u64) * 3 * n);
-    L.handles = take(sizeof(MPI_Comm_impl) * n);
-    L.dcomm = take(sizeof(DevComm));
-    L.desc = take(sizeof(DevDesc));
-    L.first = take(sizeof(int) * 2);
-    L.ptrs = take(sizeof(void*) * 2 * n);
-    L.total = take(0);
+    L.job = noalloc_take(o, sizeof(Job));
+    L.status = noalloc_take(o, sizeof(int) * 16);
+    L.err = noalloc_take(o, 256);
+    L.cs = noalloc_take(o, sizeof(CommShared));
+    L.pub = noalloc_take(o, sizeof(Pub) * (size_t)n);
+    L.flags = noalloc_take(o, sizeof(u64) * 3 * (size_t)n);
+    L.handles = noalloc_take(o, sizeof(MPI_Comm_impl) * (size_t)n);
+    L.dcomm = noalloc_take(o, sizeof(DevComm));
+    L.desc = noalloc_take(o, sizeof(DevDesc));
+    L.first = noalloc_take(o, sizeof(int) * 2);
+    L.ptrs = noalloc_take(o, sizeof(void*) * 2 * (size_t)n);
+    L.total = noalloc_take(o, 0);
     return L;
 }
+
+// The layout grows with the rank count; the largest one must fit the array
+// (a larger Job, Pub or communicator record fails the build here instead of
+// overflowing the array at run time).
+static_assert(noalloc_layout(NOALLOC_MAX_RANKS).total <= NOALLOC_SCRATCH_BYTES,
+              "allocation-free allreduce: scratch array too small for NOALLOC_MAX_RANKS");
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_dev_ptr[64];                                    // per device, looked up once
@@ -748,13 +755,22 @@ extern "C" int gpumpi_allreduce_noalloc(void* const* sendbufs, void* const* recv
         return GPUMPI_EINVAL;
     }
     if (threads_per_rank == 0) threads_per_rank = 128;
-    if (threads_per_rank < 64 || threads_per_rank > 1024 || threads_per_rank % 32) return GPUMPI_EINVAL;
+    if (threads_per_rank < 64 || threads_per_rank > 1024 || threads_per_rank % 32) {
+        set_last_error("gpumpi_allreduce_noalloc: threads_per_rank must be a multiple of 32 in [64, 1024]");
+        return GPUMPI_EINVAL;
+    }
     for (int r = 0; r < nranks; r++)
-        if (!sendbufs[r] || !recvbufs[r]) return GPUMPI_EINVAL;
+        if (!sendbufs[r] || !recvbufs[r]) {
+            set_last_error("gpumpi_allreduce_noalloc: a send or receive buffer is NULL");
+            return GPUMPI_EINVAL;
+        }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     int dev = 0;
     CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return GPUMPI_EINVAL;
+    if (dev < 0 || dev >= 64) {
+        set_last_error("gpumpi_allreduce_noalloc: device ordinal above 63");
+        return GPUMPI_EINVAL;
+    }
     if (!g_noalloc_dev_ptr[dev]) {
         void* p = nullptr;
         CK(cudaGetSymbolAddress(&p, gm_noalloc_scratch));
@@ -762,6 +778,10 @@ extern "C" int gpumpi_allreduce_noalloc(void* const* sendbufs, void* const* recv
     }
     char* base = (char*)g_noalloc_dev_ptr[dev];
     const NoallocLayout L = noalloc_layout(nranks);
+    if (L.total > NOALLOC_SCRATCH_BYTES) {   // unreachable while the static_assert holds
+        set_last_error("gpumpi_allreduce_noalloc: layout exceeds the scratch array");
+        return GPUMPI_EINVAL;
+    }
     const size_t smem = sizeof(BlockCtx) + 64;
     int per = 0, sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

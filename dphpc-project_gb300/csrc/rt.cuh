@@ -579,8 +579,8 @@ __device__ void blk_copy(void* dst, const void* src, u64 n, int tid, int T);
 // ---- bulk asynchronous copies (cp.async.bulk global -> shared -> global) ----
 // One thread drives a ring of BULK_STAGES staging buffers: a chunk is loaded
 // with cp.async.bulk into a stage (completion counted on the stage's
-// mbarrier), then stored from the stage with a bulk store; up to BULK_STAGES
-// loads are in flight while stores drain asynchronously.  Addresses and sizes
+// mbarrier), then stored from the stage with a bulk store; up to
+// BULK_STAGES - 1 loads are in flight while stores drain asynchronously.  Addresses and sizes
 // must be multiples of 16 bytes.  Every wait is bounded by the job timeout.
 __device__ u32 bulk_stage_bytes();     // staging bytes of this block (0: none)
 struct BulkPipe {

@@ -1,9 +1,9 @@
 """Host-side helpers for the GB300 device MPI runtime.
 
-Builds the CUDA runtime, the program binaries and the CPU oracle, runs
-programs through the C-ABI launcher (each program executable is a thin
-`main` around `gpumpi_main`), and binds the host collective C ABI of
-libgpumpi.so with ctypes.  The product path is the CUDA runtime: nothing here
+Builds the CUDA runtime and the program binaries, runs programs through the
+C-ABI launcher (each program executable is a thin `main` around
+`gpumpi_main`), and binds the host collective C ABI of libgpumpi.so with
+ctypes.  The product path is the CUDA runtime: nothing here
 falls back to the CPU; loading libgpumpi.so fails loudly if it is missing.
 """
 from __future__ import annotations
@@ -18,8 +18,6 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "build")
 BIN = os.path.join(BUILD, "bin")
-ORACLE = os.path.join(ROOT, "oracle")
-ORACLE_BIN = os.path.join(ORACLE, "build", "bin")
 LIB = os.path.join(BUILD, "libgpumpi.so")
 
 
@@ -28,14 +26,12 @@ def _jobs() -> int:
 
 
 def build(verbose: bool = False) -> None:
-    """Compile the CUDA runtime and programs (sm_103a) and the CPU oracle."""
+    """Compile the CUDA runtime and programs (sm_103a)."""
     out = None if verbose else subprocess.PIPE
-    for d in (PKG, ORACLE):
-        r = subprocess.run(["make", "-C", d, f"-j{_jobs()}"], stdout=out, stderr=subprocess.STDOUT,
-                           text=True)
-        if r.returncode != 0:
-            sys.stderr.write(r.stdout or "")
-            raise RuntimeError(f"build failed in {d}")
+    r = subprocess.run(["make", "-C", PKG, f"-j{_jobs()}"], stdout=out, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout or "")
+        raise RuntimeError(f"build failed in {PKG}")
 
 
 @dataclass
@@ -60,12 +56,6 @@ def run_program(name: str, args: list[str] | None = None, nranks: int = 2,
                 extra: list[str] | None = None, timeout: float = 300.0) -> RunResult:
     """Run a converted program on the GPU (one rank per thread block)."""
     return _run(os.path.join(BIN, name), args or [], nranks, extra or [], timeout)
-
-
-def run_oracle(name: str, args: list[str] | None = None, nranks: int = 2,
-               extra: list[str] | None = None, timeout: float = 300.0) -> RunResult:
-    """Run the same program on host cores through the hostmpi oracle."""
-    return _run(os.path.join(ORACLE_BIN, name), args or [], nranks, extra or [], timeout)
 
 
 def load_library() -> ctypes.CDLL:

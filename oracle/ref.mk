@@ -8,7 +8,11 @@
 #                             the source converter (_ref/conv/), so a machine
 #                             without the reference tree can build them for the
 #                             GPU and for hostmpi
-REF ?= /root/reference
+#   make -f ref.mk if-present all and conv when the reference tree exists, else
+#                             nothing (used by the build step)
+#   make -s -f ref.mk print-ref   the reference tree's path (tests read it here)
+# The reference tree: GPUMPI_REFERENCE_TREE when set, else its usual mount point.
+REF ?= $(or $(GPUMPI_REFERENCE_TREE),/root/reference)
 NPB := $(REF)/toolchain_tests/npb/NPB3.4.1/NPB3.4-MPI
 O := _ref
 CFLAGS := -O2 -ffp-contract=off -fno-fast-math -Ihostmpi/include -Dmain=hostmpi_user_main
@@ -68,4 +72,11 @@ $(C)/dt_%/npbparams.h.cuh: $(NPB)/DT/dt.c $(O)/setparams ../dphpc-project_gb300/
 	for f in DT/dt.c DT/DGraph.c common/randdp.c common/c_print_results.c common/c_timers.c; do \
 	    $(CONV) $(NPB)/$$f --project $(NPB) -I $(C)/dt_$* --outdir $(C)/npb || exit 1; done
 
-.PHONY: all conv
+print-ref:
+	@echo $(REF)
+
+if-present:
+	@if [ -d "$(REF)/toolchain_tests" ]; then $(MAKE) -f ref.mk all conv; \
+	 else echo "reference tree not found at $(REF): _ref/ not built"; fi
+
+.PHONY: all conv print-ref if-present

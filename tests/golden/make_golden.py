@@ -7,6 +7,7 @@ result line for several interval counts and rank counts.  The fixture pins
 the oracle and the GPU runtime to the reference program's output.
 
 Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+(default: the tree oracle/ref.mk names, GPUMPI_REFERENCE_TREE overriding it)
 """
 import os
 import subprocess
@@ -40,7 +41,11 @@ def run_cases(exe: str) -> list[str]:
 
 
 def main() -> None:
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 1:
+        ref_root = sys.argv[1]
+    else:
+        ref_root = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-f", "ref.mk", "print-ref"],
+                                  capture_output=True, text=True, check=True).stdout.strip()
     with tempfile.TemporaryDirectory() as d:
         lines = run_cases(build_cpi(ref_root, d))
     with open(os.path.join(HERE, "cpi_pi.txt"), "w") as f:

@@ -12,12 +12,12 @@ import subprocess
 
 import pytest
 
-from conftest import _load
+from conftest import _load, reference_tree
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CASES = os.path.join(ROOT, "tests", "convert_cases")
 ORACLE = os.path.join(ROOT, "oracle")
-REF = "/root/reference"
+REF = reference_tree()
 NVCC = "/usr/local/cuda/bin/nvcc"
 CASE_OPTS = {"globals": 0, "ring": 0, "coalesce": 3, "fileio": 0}
 
@@ -287,7 +287,7 @@ def _unstable(line):
 
 @pytest.fixture(scope="module")
 def ref_conv(oracle_built):
-    if not os.path.isdir(os.path.join(REF, "toolchain_tests")):
+    if REF is None:
         pytest.skip("reference tree absent")
     r = subprocess.run(["make", "-C", ORACLE, "-f", "ref.mk", f"REF={REF}", "all", "conv"],
                        capture_output=True, text=True)

@@ -11,8 +11,10 @@ import tempfile
 
 import pytest
 
+from conftest import reference_tree
+
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+REF = reference_tree()
 
 
 def golden():
@@ -33,7 +35,7 @@ def test_oracle_pi_matches_reference_program(oracle_built, n, ranks, line):
     assert res.lines("pi is approximately") == [line]
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "toolchain_tests", "pi")), reason="reference tree absent")
+@pytest.mark.skipif(REF is None, reason="reference tree absent")
 def test_fixture_reproduces_from_reference_source():
     import importlib.util
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "golden", "make_golden.py"))

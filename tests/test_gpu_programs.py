@@ -1,6 +1,8 @@
 """Converted programs on the GPU against the hostmpi oracle (parity gate)."""
 import pytest
 
+from conftest import run_oracle
+
 from kat_cases import KAT_CASES, check_all_ok
 
 pytestmark = pytest.mark.gpu
@@ -18,7 +20,7 @@ def test_gpu_known_answers(gpu_built, prog, scenario, nranks):
 def test_gpu_pi_bit_exact(gpu_built, n, ranks):
     """FP64 rank-order MPI_Reduce: GPU result equals the host MPI result bit for bit."""
     g = gpu_built.run_program("pi", [str(n)], nranks=ranks, extra=GPU_OPTS, timeout=180)
-    c = gpu_built.run_oracle("pi", [str(n)], nranks=ranks, timeout=180)
+    c = run_oracle("pi", [str(n)], nranks=ranks, timeout=180)
     assert g.returncode == 0, g.stderr
     assert g.lines("pi bits") == c.lines("pi bits")
     assert g.lines("pi is approximately") == c.lines("pi is approximately")
@@ -29,7 +31,7 @@ def test_gpu_coll_bench_matches_oracle(gpu_built, lg, iters, ranks):
     """Batched-collectives program: every result checksum equals the host MPI run."""
     g = gpu_built.run_program("coll_bench", [str(lg), str(iters)], nranks=ranks,
                               extra=GPU_OPTS + ["-p", "4G"], timeout=300)
-    c = gpu_built.run_oracle("coll_bench", [str(lg), str(iters)], nranks=ranks, timeout=300)
+    c = run_oracle("coll_bench", [str(lg), str(iters)], nranks=ranks, timeout=300)
     assert g.returncode == 0, g.stderr[-2000:]
     assert c.returncode == 0, c.stderr[-2000:]
     assert g.lines("coll_bench checksum") == c.lines("coll_bench checksum")
@@ -54,7 +56,7 @@ def test_gpu_p2p_sweep_matches_oracle(gpu_built, pattern, mode, lo, hi, iters, r
     MPI_COMM_WORLD and on a duplicate of it."""
     args = [pattern, mode, str(lo), str(hi), str(iters), comm]
     g = gpu_built.run_program("p2p_sweep", args, nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=300)
-    c = gpu_built.run_oracle("p2p_sweep", args, nranks=ranks, timeout=300)
+    c = run_oracle("p2p_sweep", args, nranks=ranks, timeout=300)
     assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
     assert c.returncode == 0, c.stderr[-2000:]
     got = g.lines("p2p ")
@@ -69,7 +71,7 @@ def test_gpu_is_sort_matches_oracle(gpu_built, args, ranks):
     """IS-like bucket sort: globally sorted, and every per-iteration checksum and
     the sorted-key checksum equal the host MPI run's."""
     g = gpu_built.run_program("is_sort", args, nranks=ranks, extra=GPU_OPTS + ["-p", "2G"], timeout=300)
-    c = gpu_built.run_oracle("is_sort", args, nranks=ranks, timeout=300)
+    c = run_oracle("is_sort", args, nranks=ranks, timeout=300)
     assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
     assert c.returncode == 0, c.stderr[-2000:]
     assert g.lines("is verify")[0].endswith("PASSED")
@@ -93,7 +95,7 @@ def test_gpu_pic_matches_oracle(gpu_built, args, ranks, heap):
     stated tolerance; the arithmetic is + - * / only, so they agree bit for
     bit) and the same particle count and position checksum."""
     g = gpu_built.run_program("pic", args, nranks=ranks, extra=GPU_OPTS + ["-p", heap], timeout=600)
-    c = gpu_built.run_oracle("pic", args, nranks=ranks, timeout=600)
+    c = run_oracle("pic", args, nranks=ranks, timeout=600)
     assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
     assert c.returncode == 0, c.stderr[-2000:]
     gv, cv = _pic_values(g), _pic_values(c)

@@ -14,9 +14,11 @@ import subprocess
 
 import pytest
 
+from conftest import reference_tree
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "toolchain_tests")),
+REF = reference_tree()
+pytestmark = pytest.mark.skipif(REF is None,
                                 reason="reference tree absent")
 
 
