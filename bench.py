@@ -54,8 +54,9 @@ def load_peaks():
 class ClockSampler:
     """nvidia-smi samples during the timed region."""
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, interval_ms: int = 20):
         self.gpu = gpu
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines: list[str] = []
 
@@ -66,7 +67,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
             t0 = time.time()
@@ -121,6 +122,12 @@ NCU_TRAFFIC_BYTES_2_15 = 0.979630336e9 + 1.461430e9
 ALL_KINDS = ("bcast", "allreduce", "alltoall")
 
 
+def a2a_per(n: int, p: int) -> int:
+    """Elements each rank sends to each peer in the Alltoall of a rank with n
+    elements: n / P (at least 1, so that small counts still move data)."""
+    return max(1, n // p)
+
+
 def alg_bytes(sizes, n, kinds=ALL_KINDS):
     total = 0
     for p in sizes:
@@ -129,7 +136,7 @@ def alg_bytes(sizes, n, kinds=ALL_KINDS):
                 total += p * n * s              # Bcast
             if "allreduce" in kinds:
                 total += 2 * p * n * s          # Allreduce
-            per = n // p
+            per = a2a_per(n, p)
             if "alltoall" in kinds:
                 total += 2 * p * p * per * s    # Alltoall
     return total
@@ -169,7 +176,7 @@ def build_plan(coll, lib, torch, sizes, n, batched, threads, seed=1, kinds=ALL_K
     for p in sizes:
         c = coll.Comm(lib, p)
         comms.append(c)
-        per = n // p
+        per = a2a_per(n, p)
         for dt, tdt in (("int32", torch.int32), ("float64", torch.float64)):
             es = 4 if dt == "int32" else 8
 
@@ -263,6 +270,133 @@ def time_plan(torch, plan, steps, warmup, stream):
     return e0.elapsed_time(e1) / 1000.0
 
 
+def sweep_point(coll, lib, torch, lg: int, stream, peak: float, tune_reps: int, target_s: float = 0.05,
+                sync_mode: int = 0):
+    """The workload at 2^lg elements per rank: tuned batched plan (CUDA graph)
+    against the tuned plain form, results checked after timing."""
+    n = 1 << lg
+    plan, comms, keep, items, descs = build_plan(coll, lib, torch, COMM_SIZES, n, True, 128, seed=40 + lg)
+    plan.close()
+    threads, pth, palg = coll.autotune(lib, descs, reps=tune_reps)
+    plan = coll.Plan(lib, descs, threads=threads, batched=True)
+    g = torch.Generator(device="cuda").manual_seed(60 + lg)
+    for it in items:
+        fill_random(torch, it.send if it.send is not None else it.recv, it.dt, g)
+    if sync_mode:
+        plan.set_sync(sync_mode)
+    plan.capture(stream.cuda_stream)
+    t1 = time_plan(torch, plan, 3, 3, stream) / 3
+    steps = int(min(2000, max(10, target_s / max(t1, 1e-7))))
+    secs = time_plan(torch, plan, steps, 0, stream)
+    bad = verify_items(torch, items, sample=1024)
+    if bad or coll.status(lib):
+        raise SystemExit(f"sweep 2^{lg}: result mismatch or device error: {bad[:4]}")
+    ordered = plan.launch_ordered
+    plan.close()
+    pdescs = [type(d).from_buffer_copy(d) for d in descs]
+    for d, a in zip(pdescs, palg):
+        d.algo = a
+    plain = coll.Plan(lib, pdescs, threads=threads, batched=False, plain_threads=pth)
+    if sync_mode:
+        plain.set_sync(sync_mode)
+    p1 = time_plan(torch, plain, 1, 1, stream)
+    psteps = int(min(200, max(3, target_s / max(p1, 1e-7))))
+    psecs = time_plan(torch, plain, psteps, 0, stream)
+    plain.close()
+    for c in comms:
+        c.close()
+    nbytes = alg_bytes(COMM_SIZES, n)
+    per_step = secs / steps
+    gbs = nbytes / per_step / 1e9
+    pgbs = nbytes * psteps / psecs / 1e9
+    del items
+    torch.cuda.empty_cache()
+    return {"elements_per_rank": n, "value": round(gbs, 2), "unit": "GB/s", "frac": round(gbs / peak, 4),
+            "us_per_step": round(per_step * 1e6, 2), "steps": steps, "threads_per_rank": threads,
+            "launch_ordered": bool(ordered), "tuned_plain_value": round(pgbs, 2),
+            "batched_over_tuned_plain": round(gbs / pgbs, 2), "verified": True,
+            "l2_resident": nbytes < 120e6}
+
+
+# Application runs (extra key `apps`): the programs of the other benchmark
+# configurations, on the GPU and on the host cores through hostmpi in the same
+# run.  (name, program, arguments, ranks, GPU launcher options, time pattern)
+APPS = [
+    ("pi_1e7_8ranks", "pi", ["10000000"], 8, [], r"wall clock time = ([0-9.]+)"),
+    ("p2p_pair_8B_blocking", "p2p_sweep", ["pairs", "block", "3", "3", "2000"], 2, [],
+     r"p2p-time bytes \d+ seconds ([0-9.]+)"),
+    ("p2p_pair_1MiB_nonblocking", "p2p_sweep", ["pairs", "nb", "20", "20", "200"], 2, [],
+     r"p2p-time bytes \d+ seconds ([0-9.]+)"),
+    ("p2p_pair_64MiB_nonblocking", "p2p_sweep", ["pairs", "nb", "26", "26", "10"], 2, ["-p", "2G"],
+     r"p2p-time bytes \d+ seconds ([0-9.]+)"),
+    ("p2p_ring_1024ranks_1MiB", "p2p_sweep", ["ring", "nb", "20", "20", "10"], 1024, ["-p", "8G"],
+     r"p2p-time bytes \d+ seconds ([0-9.]+)"),
+    ("is_like_sort_2e23_64ranks", "is_sort", ["23", "10"], 64, ["-p", "2G"], r"is-time seconds ([0-9.]+)"),
+    ("pic_64ranks_50cycles", "pic", ["50"], 64, ["-p", "4G"], r"pic-time seconds ([0-9.]+)"),
+]
+TIME_LINE = re.compile(r"^(wall clock time|p2p-time|is-time|pic-time)")
+
+
+def _pic_rel(a: list[str], b: list[str]) -> float:
+    """Largest relative difference of the energies printed by two PIC runs."""
+    worst = 0.0
+    for x, y in zip(a, b):
+        fx, fy = x.split(), y.split()
+        for u, v in zip(fx, fy):
+            try:
+                fu, fv = float(u), float(v)
+            except ValueError:
+                continue
+            if "e" in u or "." in u:
+                worst = max(worst, abs(fu - fv) / max(abs(fv), 1e-300))
+    return worst
+
+
+def app_runs(host, timeout: float = 600.0) -> dict:
+    """Each program once on the GPU and once on hostmpi; wall times of the
+    programs' own timed regions (MPI_Wtime brackets, slowest rank) and whether
+    the results agree (every printed result line, timing lines aside)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("hostmpi_run", os.path.join(ROOT, "oracle", "hostmpi_run.py"))
+    oracle = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(oracle)
+    out = {}
+    for name, prog, pargs, ranks, extra, pat in APPS:
+        rec = {"ranks": ranks, "args": " ".join(pargs)}
+        try:
+            g = host.run_program(prog, pargs, nranks=ranks, extra=["--timeout-ms", "60000", *extra], timeout=timeout)
+            c = oracle.run_oracle(prog, pargs, nranks=ranks, timeout=timeout)
+            mg, mc = re.search(pat, g.stdout), re.search(pat, c.stdout)
+            if g.returncode or not mg:
+                raise RuntimeError(f"GPU run failed: {g.stderr[-300:]}")
+            if c.returncode or not mc:
+                raise RuntimeError(f"hostmpi run failed: {c.stderr[-300:]}")
+            rg = [ln for ln in g.stdout.splitlines() if ln.strip() and not TIME_LINE.match(ln)]
+            rc = [ln for ln in c.stdout.splitlines() if ln.strip() and not TIME_LINE.match(ln)]
+            gs, cs = float(mg.group(1)), float(mc.group(1))
+            rec.update({"gpu_s": gs, "hostmpi_s": cs, "hostmpi_cores": os.cpu_count(),
+                        "hostmpi_over_gpu": round(cs / gs, 2) if gs > 0 else None})
+            if prog == "p2p_sweep":
+                iters = int(pargs[4])
+                rec["gpu_us_per_iter"] = round(1e6 * gs / iters, 3)
+                rec["hostmpi_us_per_iter"] = round(1e6 * cs / iters, 3)
+                mb = re.search(r"GBps ([0-9.]+)", g.stdout)
+                rec["gpu_GBps"] = float(mb.group(1)) if mb else None
+            if rg == rc:
+                rec["parity"] = "result lines identical"
+            elif prog == "pic" and len(rg) == len(rc):
+                rel = _pic_rel(rg, rc)
+                rec["parity"] = f"energies within {rel:.2e} relative"
+                if rel > 1e-10:
+                    raise RuntimeError(f"PIC energies differ by {rel:.3e} relative")
+            else:
+                raise RuntimeError("results differ from hostmpi: " + str([x for x in rg if x not in rc][:3]))
+        except Exception as e:  # reported in the line, and the run fails below
+            rec["error"] = str(e)[:400]
+        out[name] = rec
+    return out
+
+
 def run_oracle_bench(lg: int, iters: int, ranks: int = 1024, timeout: float = 900):
     exe = os.path.join(ROOT, "oracle", "build", "bin", "coll_bench")
     if not os.path.exists(exe):
@@ -319,8 +453,15 @@ def main():
     ap.add_argument("--cpu-lg", type=int, default=16)
     ap.add_argument("--cpu-iters", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-apps", action="store_true", help="skip the application runs (extra key apps)")
+    ap.add_argument("--sustain-s", type=float, default=3.0,
+                    help="seconds of extra replays after the timed region (extra key sustained; 0 = none)")
     ap.add_argument("--no-tune", action="store_true", help="built-in schedules, --threads for every launch")
     ap.add_argument("--tune-reps", type=int, default=3)
+    ap.add_argument("--sync-mode", type=int, default=0,
+                    help="0: launch-ordered forms when the calls are independent; 1: flag rounds (diagnostic)")
+    ap.add_argument("--sweep", default="0,4,8,12,15,17",
+                    help="log2 elements per rank of the size sweep (extra key; empty = none)")
     ap.add_argument("--verify-sample", type=int, default=4096,
                     help="element positions per Allreduce checked after the timed region")
     ap.add_argument("--kinds", default=",".join(ALL_KINDS),
@@ -379,6 +520,8 @@ def main():
         g = torch.Generator(device="cuda").manual_seed(11)
         for it in items:
             fill_random(torch, it.send if it.send is not None else it.recv, it.dt, g)
+    if args.sync_mode:
+        plan.set_sync(args.sync_mode)
     plan.capture(stream.cuda_stream)
     launches0 = lib.gpumpi_kernel_launches()
     with torch.cuda.stream(stream):
@@ -397,10 +540,20 @@ def main():
     with ClockSampler(local) as clocks:
         secs = time_plan(torch, plan, args.steps, 0, stream)
     launches = lib.gpumpi_kernel_launches() - launches0 - args.warmup - int(args.profile_launch)
+    ordered = plan.launch_ordered
     err = coll.status(lib)
     if err:
         raise SystemExit(f"device error during benchmark: {err}")
     secs = max_over_ranks(dist, torch, secs)
+    # the same launch replayed for a few seconds more, clocks sampled: the
+    # rate holds beyond the short timed region
+    sustained = None
+    if args.sustain_s > 0:
+        ssteps = max(args.steps, int(args.sustain_s * args.steps / max(secs, 1e-9)))
+        with ClockSampler(local, interval_ms=100) as sclocks:
+            ssecs = time_plan(torch, plan, ssteps, 0, stream)
+        sustained = {"value": round(alg_bytes(COMM_SIZES, n, kinds) * ssteps / ssecs / 1e9, 2), "unit": "GB/s",
+                     "steps": ssteps, "seconds": round(ssecs, 3), "clocks": sclocks.summary()}
     # outside the timed region: every call's result against its inputs, bit
     # for bit (reductions at sampled element positions of every rank)
     t0 = time.perf_counter()
@@ -418,6 +571,8 @@ def main():
     # structure is the only difference), then with each launch's own tuned
     # schedule and thread count (a small communicator may use 1024 threads per rank)
     plain = coll.Plan(lib, descs, threads=threads, batched=False)
+    if args.sync_mode:
+        plain.set_sync(args.sync_mode)
     psecs = time_plan(torch, plain, args.plain_steps, 1, stream)
     plain_gbs = nbytes * args.plain_steps / psecs / 1e9
     plain.close()
@@ -427,6 +582,8 @@ def main():
         for d, a in zip(pdescs, plain_algos):
             d.algo = a
         plain = coll.Plan(lib, pdescs, threads=threads, batched=False, plain_threads=plain_threads)
+        if args.sync_mode:
+            plain.set_sync(args.sync_mode)
         psecs = time_plan(torch, plain, args.plain_steps, 1, stream)
         plain_tuned_gbs = nbytes * args.plain_steps / psecs / 1e9
         plain.close()
@@ -488,6 +645,25 @@ def main():
         ep.close()
     del eparts
 
+    # the same workload over the configuration's range of elements per rank
+    sweep = []
+    for tok in [t for t in args.sweep.split(",") if t.strip()]:
+        lg = int(tok)
+        if lg == args.lg:
+            continue
+        sweep.append(sweep_point(coll, lib, torch, lg, stream, peak, tune_reps=1, sync_mode=args.sync_mode))
+    if kinds == ALL_KINDS:
+        sweep.append({"elements_per_rank": n, "value": round(kernel_gbs, 2), "unit": "GB/s",
+                      "frac": round(kernel_gbs / peak, 4), "us_per_step": round(per_step * 1e6, 2),
+                      "steps": args.steps, "threads_per_rank": threads, "launch_ordered": bool(ordered),
+                      "tuned_plain_value": round(plain_tuned_gbs, 2) if plain_tuned_gbs else None,
+                      "batched_over_tuned_plain": round(kernel_gbs / plain_tuned_gbs, 2) if plain_tuned_gbs else None,
+                      "sustained": sustained,
+            "sweep": sweep,
+            "apps": apps,
+            "verified": True, "l2_resident": False})
+    sweep.sort(key=lambda d: d["elements_per_rank"])
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -498,6 +674,10 @@ def main():
         except Exception as e:  # reported, not fatal
             cpu = {"value": None, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
+
+    apps = None
+    if rank == 0 and not args.no_apps:
+        apps = app_runs(host)
 
     if rank == 0:
         line = {
@@ -516,7 +696,9 @@ def main():
             "config": {"workload": WORKLOAD if kinds == ALL_KINDS else
                        "diagnostic subset of the batched collectives: " + "+".join(kinds),
                        "elements_per_rank": n, "comm_sizes": COMM_SIZES,
-                       "threads_per_rank": threads, "form": "batched, CUDA graph replay",
+                       "threads_per_rank": threads,
+                       "form": "batched, CUDA graph replay, " + ("launch-ordered (independent calls, no flag rounds)"
+                                                                  if ordered else "flag rounds"),
                        "tuning": tuning,
                        "l2": "inputs larger than L2 (each step touches ~%.0f GB)" % (nbytes / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -548,6 +730,9 @@ def main():
             "gpu_launches": int(launches),
         }
         print(json.dumps(line), flush=True)
+        bad_apps = [k for k, v in (apps or {}).items() if "error" in v]
+        if bad_apps:
+            raise SystemExit("application runs failed: " + ", ".join(bad_apps))
     for c in comms + ecomms:
         c.close()
     if dist:

@@ -34,6 +34,7 @@ struct DevDesc {
     int pad;
     void** sbufs;   // [P] device array
     void** rbufs;   // [P]
+    const Pub* pub; // [P] buffer table of the launch-ordered forms (nullptr: none)
 };
 
 struct DevComm {
@@ -49,9 +50,12 @@ struct PlanArgs {
     const int* slot_comm;     // [nslots], nullptr = every block in communicator 0
     const int* slot_rank;     // [nslots], nullptr = rank is blockIdx.x
     const DevComm* comms;
+    int ordered;              // 1: the launch-ordered forms (calls touch disjoint memory)
+    int pad;
 };
 
-static __device__ int run_desc(const DevDesc& d, MPI_Comm_impl* comm, int rank, int tid, int T) {
+static __device__ int run_desc(const DevDesc& d, MPI_Comm_impl* comm, int P, int rank, int ordered, int tid,
+                               int T) {
     CollArgs a;
     memset(&a, 0, sizeof(a));
     a.comm = comm;
@@ -64,6 +68,26 @@ static __device__ int run_desc(const DevDesc& d, MPI_Comm_impl* comm, int rank, 
     a.ufn = nullptr;
     const void* sb = d.sbufs ? ldcg(&d.sbufs[rank]) : nullptr;
     void* rb = d.rbufs ? ldcg(&d.rbufs[rank]) : nullptr;
+    if (ordered && d.pub) {
+        a.sbuf = sb;
+        a.rbuf = rb;
+        switch (d.op) {
+            case GPUMPI_COLL_BCAST:
+                a.count = d.count * d.esize;
+                return coll_lo_bcast(a, d.pub, P, rank, tid, T);
+            case GPUMPI_COLL_REDUCE:
+                a.count = d.count;
+                return coll_lo_reduce(a, d.pub, P, rank, tid, T);
+            case GPUMPI_COLL_ALLREDUCE:
+                a.count = d.count;
+                return coll_lo_allreduce(a, d.pub, P, rank, tid, T);
+            case GPUMPI_COLL_ALLTOALL:
+            case GPUMPI_COLL_ALLGATHER:
+                a.count = d.count;
+                return coll_lo_alltoall(a, d.pub, P, rank, d.op == GPUMPI_COLL_ALLGATHER, tid, T);
+            default: break;   // a barrier keeps its flag round
+        }
+    }
     switch (d.op) {
         case GPUMPI_COLL_BARRIER: return coll_barrier(comm, tid, T);
         case GPUMPI_COLL_BCAST:
@@ -116,8 +140,9 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_plan_kernel(PlanArgs A
     __syncthreads();
     MPI_Comm_impl* comm = &A.comms[c].handles[rank];
     const int tid = (int)threadIdx.x, T = (int)blockDim.x;
+    const int P = A.comms[c].size;
     for (int i = A.comm_first[c]; i < A.comm_first[c + 1]; i++) {
-        if (run_desc(A.descs[i], comm, rank, tid, T) != MPI_SUCCESS) break;
+        if (run_desc(A.descs[i], comm, P, rank, A.ordered, tid, T) != MPI_SUCCESS) break;
     }
 }
 
@@ -150,6 +175,9 @@ struct gpumpi_plan_s {
     cudaGraphExec_t exec = nullptr;
     std::vector<gpumpi_coll_desc> descs;   // host copies for the host-buffer path
     std::vector<std::vector<void*>> sb, rb;
+    int independent = 0;                   // calls touch disjoint memory and include no barrier
+    int sync_mode = 0;                     // 0 automatic, 1 flag rounds for every call
+    std::vector<int> plain_op;             // collective of each plain launch
 };
 
 namespace {
@@ -219,6 +247,65 @@ void desc_bytes(const gpumpi_coll_desc& d, int P, size_t* in, size_t* out) {
         case GPUMPI_COLL_ALLGATHER: *in = e; *out = e * P; break;
         default: *in = *out = 0;
     }
+}
+
+// True when no call of the list writes memory that another call reads or
+// writes (and none is a barrier): the plan kernel may then run every call in
+// its launch-ordered form.  Each call's spans: the bytes each rank reads and
+// writes (Bcast: the root's buffer is read, the others written).  Spans of one
+// call never conflict with each other here (in-place forms are the
+// schedules' concern); spans are sorted by start and compared with the spans
+// still open.
+bool plan_independent(const gpumpi_coll_desc* descs, int ndesc) {
+    struct Span {
+        uintptr_t lo, hi;
+        int call, w;
+    };
+    std::vector<Span> v;
+    for (int i = 0; i < ndesc; i++) {
+        const gpumpi_coll_desc& d = descs[i];
+        if (d.op == GPUMPI_COLL_BARRIER) return false;
+        const int P = d.comm->n;
+        const size_t e = (size_t)esize_of(d.dtype) * d.count;
+        auto add = [&](void* const* tab, int r, size_t bytes, int w) {
+            const void* p = tab ? tab[r] : nullptr;
+            if (p && bytes) v.push_back({(uintptr_t)p, (uintptr_t)p + bytes, i, w});
+        };
+        for (int r = 0; r < P; r++) {
+            switch (d.op) {
+                case GPUMPI_COLL_BCAST: add(d.recvbufs, r, e, r != d.root); break;
+                case GPUMPI_COLL_REDUCE:
+                    add(d.sendbufs, r, e, 0);
+                    if (r == d.root) add(d.recvbufs, r, e, 1);
+                    break;
+                case GPUMPI_COLL_ALLREDUCE:
+                    add(d.sendbufs, r, e, 0);
+                    add(d.recvbufs, r, e, 1);
+                    break;
+                case GPUMPI_COLL_ALLTOALL:
+                    add(d.sendbufs, r, e * P, 0);
+                    add(d.recvbufs, r, e * P, 1);
+                    break;
+                case GPUMPI_COLL_ALLGATHER:
+                    add(d.sendbufs, r, e, 0);
+                    add(d.recvbufs, r, e * P, 1);
+                    break;
+                default: break;
+            }
+        }
+    }
+    std::sort(v.begin(), v.end(), [](const Span& a, const Span& b) { return a.lo < b.lo; });
+    std::vector<Span> open;
+    for (const Span& x : v) {
+        size_t k = 0;
+        for (size_t j = 0; j < open.size(); j++)
+            if (open[j].hi > x.lo) open[k++] = open[j];
+        open.resize(k);
+        for (const Span& o : open)
+            if (o.call != x.call && (o.w || x.w)) return false;
+        open.push_back(x);
+    }
+    return true;
 }
 
 int launch(const void* kern, int grid, int threads, size_t smem, PlanArgs* args, cudaStream_t st) {
@@ -353,14 +440,16 @@ extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, i
     size_t off_pp = off_cm + sizeof(DevComm) * ncomm;
     size_t off_pc = (off_pp + sizeof(int) * 2 * ndesc + 15) & ~(size_t)15;
     size_t off_ptr = off_pc + sizeof(DevComm) * ndesc;
-    size_t total = off_ptr + sizeof(void*) * ptrs + 16;
+    size_t off_pubt = (off_ptr + sizeof(void*) * ptrs + 63) & ~(size_t)63;   // Pub tables, one entry per rank
+    size_t total = off_pubt + sizeof(Pub) * (ptrs / 2) + 16;
     gpumpi_plan_s* p = new gpumpi_plan_s();
     CK(cudaMalloc(&p->base, total));
     char* base = p->base;
     std::vector<char> h(total, 0);
     DevDesc* hd = (DevDesc*)(h.data() + off_desc);
     void** hp = (void**)(h.data() + off_ptr);
-    size_t pk = 0;
+    Pub* hpub = (Pub*)(h.data() + off_pubt);
+    size_t pk = 0, pubk = 0;
     p->descs.assign(descs, descs + ndesc);
     p->sb.resize(ndesc);
     p->rb.resize(ndesc);
@@ -383,6 +472,14 @@ extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, i
         for (int r = 0; r < P; r++) hp[pk++] = d.recvbufs ? d.recvbufs[r] : nullptr;
         p->sb[i].assign(hp + pk - 2 * P, hp + pk - P);
         p->rb[i].assign(hp + pk - P, hp + pk);
+        x.pub = (const Pub*)(base + off_pubt) + pubk;
+        for (int r = 0; r < P; r++, pubk++) {
+            Pub& e = hpub[pubk];
+            e.rbuf = d.recvbufs ? d.recvbufs[r] : nullptr;
+            e.sbuf = d.sendbufs ? d.sendbufs[r] : e.rbuf;
+            e.a0 = (long long)d.count;
+            e.a1 = x.esize;
+        }
     }
     memcpy(h.data() + off_cf, comm_first.data(), sizeof(int) * (ncomm + 1));
     int* sc = (int*)(h.data() + off_sc);
@@ -417,6 +514,9 @@ extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, i
     p->batch_args.slot_comm = (const int*)(base + off_sc);
     p->batch_args.slot_rank = (const int*)(base + off_sr);
     p->batch_args.comms = (const DevComm*)(base + off_cm);
+    p->independent = plan_independent(descs, ndesc) ? 1 : 0;
+    p->batch_args.ordered = p->independent;
+    p->batch_args.pad = 0;
     p->plain_args.resize(ndesc);
     p->plain_grid.resize(ndesc);
     p->plain_threads.resize(ndesc);
@@ -430,6 +530,9 @@ extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, i
         a.slot_comm = nullptr;
         a.slot_rank = nullptr;
         a.comms = (const DevComm*)(base + off_pc) + k;
+        a.ordered = hd[k].op != GPUMPI_COLL_BARRIER;   // one call per launch: always launch-ordered
+        a.pad = 0;
+        p->plain_op.push_back(hd[k].op);
         p->plain_grid[k] = comms[hd[k].comm]->n;
     }
     // co-residency: every rank block of one launch must fit on the GPU at once
@@ -480,6 +583,25 @@ extern "C" int gpumpi_plan_launch(gpumpi_plan_t p, void* stream) {
         return GPUMPI_OK;
     }
     return plan_enqueue(p, st);
+}
+
+extern "C" int gpumpi_plan_set_sync(gpumpi_plan_t p, int mode) {
+    if (!p || mode < 0 || mode > 1) return GPUMPI_EINVAL;
+    p->sync_mode = mode;
+    p->batch_args.ordered = mode == 0 && p->independent;
+    for (int k = 0; k < p->ndesc; k++)
+        p->plain_args[k].ordered = mode == 0 && p->plain_op[k] != GPUMPI_COLL_BARRIER;
+    // a captured graph holds the old launch arguments: launch eagerly until captured again
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->exec = nullptr;
+    p->graph = nullptr;
+    return GPUMPI_OK;
+}
+
+extern "C" int gpumpi_plan_launch_ordered(gpumpi_plan_t p) {
+    if (!p) return 0;
+    return p->batched ? p->batch_args.ordered : (p->sync_mode == 0);
 }
 
 extern "C" int gpumpi_plan_capture(gpumpi_plan_t p, void* stream) {
@@ -847,6 +969,8 @@ extern "C" int gpumpi_allreduce_noalloc(void* const* sendbufs, void* const* recv
     args.slot_comm = nullptr;
     args.slot_rank = nullptr;
     args.comms = (const DevComm*)(base + L.dcomm);
+    args.ordered = 0;
+    args.pad = 0;
     int rc = launch((const void*)gpumpi_plan_kernel, nranks, threads_per_rank, smem, &args, st);
     if (rc) return rc;
     CK(cudaStreamSynchronize(st));

@@ -465,6 +465,115 @@ __device__ int coll_scan(const CollArgs& a, int exclusive, int tid, int T) {
     return wait_flags_ge(cs->depart, P, seq, me, tid, T);
 }
 
+// ---------------------------------------------------------------- launch-ordered forms
+// A host plan whose calls touch disjoint memory (the plan checks every pair of
+// calls on the host) needs no arrive and no depart round: every input was
+// written before the launch started (stream order), no call of the launch
+// writes what another reads, and the end of the launch orders every result
+// before whatever follows it on the stream.  These forms therefore read the
+// peers' buffers from a table the plan built on the host (`pub`, one entry per
+// rank) and synchronise nothing but their own rank block, so a rank never waits
+// for a slower peer.  The one exception is the reduce-scatter + allgather
+// Allreduce: its allgather reads what the reduce-scatter wrote in the same
+// launch, so it keeps its middle flag round.  The arithmetic and the fold
+// order are those of the synchronised forms above.
+
+// Bcast: a.rbuf of every rank receives a.count bytes of the root's.
+__device__ int coll_lo_bcast(const CollArgs& a, const Pub* pub, int P, int me, int tid, int T) {
+    if (P > 1 && me != a.root && a.count) blk_copy(a.rbuf, ldcg(&pub[a.root].rbuf), a.count, tid, T);
+    bsync();
+    return MPI_SUCCESS;
+}
+
+// Reduce to a.root (a.sbuf == a.rbuf at the root works in place).
+__device__ int coll_lo_reduce(const CollArgs& a, const Pub* pub, int P, int me, int tid, int T) {
+    const int es = a.rsize;
+    const u64 n = a.count;
+    if (P == 1) {
+        if (a.sbuf != a.rbuf) blk_copy(a.rbuf, a.sbuf, n * es, tid, T);
+        bsync();
+        return MPI_SUCCESS;
+    }
+    const bool root_only = (a.algo == 1) || (a.algo == 0 && n * es * (u64)P <= REDUCE_ROOT_ONLY_BYTES);
+    if (root_only) {
+        if (me == a.root) fold_range(a.opi, a.ufn, a.dtype, es, a.rbuf, pub, P, 0, 0, n, tid, T);
+        bsync();
+        return MPI_SUCCESS;
+    }
+    const u64 per = seg_len(n, P, es);
+    u64 lo = (u64)me * per;
+    if (lo > n) lo = n;
+    u64 hi = lo + per;
+    if (hi > n) hi = n;
+    char* out = (char*)ldcg(&pub[a.root].rbuf) + lo * es;
+    if (hi > lo) fold_range(a.opi, a.ufn, a.dtype, es, out, pub, P, 0, lo, hi, tid, T);
+    bsync();
+    return MPI_SUCCESS;
+}
+
+// Allreduce (a.sbuf == a.rbuf works in place).
+__device__ int coll_lo_allreduce(const CollArgs& a, const Pub* pub, int P, int me, int tid, int T) {
+    const int es = a.rsize;
+    const u64 n = a.count;
+    const bool in_place = a.sbuf == a.rbuf;
+    if (P == 1) {
+        if (!in_place) blk_copy(a.rbuf, a.sbuf, n * es, tid, T);
+        bsync();
+        return MPI_SUCCESS;
+    }
+    const bool direct = (a.algo == 1) || (a.algo == 0 && n * es <= ALLREDUCE_DIRECT_BYTES);
+    if (direct && !in_place) {
+        // every rank folds every input into its own receive buffer
+        fold_range(a.opi, a.ufn, a.dtype, es, a.rbuf, pub, P, 0, 0, n, tid, T);
+        return MPI_SUCCESS;
+    }
+    const u64 per = seg_len(n, P, es);
+    u64 lo = (u64)me * per;
+    if (lo > n) lo = n;
+    u64 hi = lo + per;
+    if (hi > n) hi = n;
+    if (a.algo != 2 && fold_range_push(a.opi, a.dtype, pub, P, lo, hi, tid, T)) return MPI_SUCCESS;
+    // reduce-scatter into the owner's receive buffer, one flag round, allgather
+    const BlockCtx::CommView* cs = &bctx().cv;
+    const u64 seq = coll_begin(a.comm, tid);
+    if (hi > lo) fold_range(a.opi, a.ufn, a.dtype, es, (char*)a.rbuf + lo * es, pub, P, 0, lo, hi, tid, T);
+    raise_flag(cs->mid, me, seq, tid);
+    const int rc = wait_flags_ge(cs->mid, P, seq, me, tid, T);
+    if (rc) return rc;
+    auto seg = [&](int q, const void** s, void** d, u64* nb) -> bool {
+        if (q == me) return false;
+        u64 l = (u64)q * per;
+        if (l >= n) return false;
+        u64 h = l + per;
+        if (h > n) h = n;
+        *s = (const char*)ldcg(&pub[q].rbuf) + l * es;
+        *d = (char*)a.rbuf + l * es;
+        *nb = (h - l) * es;
+        return true;
+    };
+    multi_copy(P, me + 1, per * es, seg, tid, T);
+    return MPI_SUCCESS;
+}
+
+// Alltoall / Allgather with a uniform block of a.count elements of a.rsize
+// bytes: block q of this rank's a.rbuf comes from rank q (Alltoall: its block
+// for this rank; Allgather: its whole send buffer).
+__device__ int coll_lo_alltoall(const CollArgs& a, const Pub* pub, int P, int me, int gather, int tid, int T) {
+    const u64 b = a.count * (u64)a.rsize;
+    if (b == 0) {
+        bsync();
+        return MPI_SUCCESS;
+    }
+    auto blk = [&](int q, const void** s, void** d, u64* nb) -> bool {
+        *s = (const char*)ldcg(&pub[q].sbuf) + (gather ? 0 : (u64)me * b);
+        *d = (char*)a.rbuf + (u64)q * b;
+        *nb = b;
+        return true;
+    };
+    multi_copy(P, me, b, blk, tid, T, a.algo);
+    return MPI_SUCCESS;
+}
+
 // ---------------------------------------------------------------- communicator creation
 static __device__ CommShared* arena_comm(Job* j, int size) {
     u64 bytes = sizeof(CommShared) + (u64)size * (sizeof(int) + sizeof(Pub) + 3 * sizeof(u64)) + 256;

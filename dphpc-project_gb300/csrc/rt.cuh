@@ -667,6 +667,12 @@ __device__ int coll_alltoallv(const CollArgs& a, int tid, int T);
 __device__ int coll_alltoall(const CollArgs& a, int tid, int T);
 __device__ int coll_reduce_scatter_block(const CollArgs& a, int tid, int T);
 __device__ int coll_scan(const CollArgs& a, int exclusive, int tid, int T);
+// Launch-ordered forms for host plans whose calls touch disjoint memory (no
+// arrive/depart flags; `pub` is the call's buffer table, one entry per rank).
+__device__ int coll_lo_bcast(const CollArgs& a, const Pub* pub, int P, int me, int tid, int T);
+__device__ int coll_lo_reduce(const CollArgs& a, const Pub* pub, int P, int me, int tid, int T);
+__device__ int coll_lo_allreduce(const CollArgs& a, const Pub* pub, int P, int me, int tid, int T);
+__device__ int coll_lo_alltoall(const CollArgs& a, const Pub* pub, int P, int me, int gather, int tid, int T);
 __device__ int comm_split_block(MPI_Comm_impl* parent, int color, int key, MPI_Comm_impl** out,
                                 int tid, int T);
 

@@ -36,6 +36,8 @@ def bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     lib.gpumpi_autotune.argtypes = [POINTER(Desc), c_int, c_void_p, POINTER(c_int), POINTER(c_int), POINTER(c_int)]
     lib.gpumpi_plan_launch.argtypes = [c_void_p, c_void_p]
     lib.gpumpi_plan_capture.argtypes = [c_void_p, c_void_p]
+    lib.gpumpi_plan_set_sync.argtypes = [c_void_p, c_int]
+    lib.gpumpi_plan_launch_ordered.argtypes = [c_void_p]
     lib.gpumpi_plan_run_host.argtypes = [c_void_p, POINTER(c_void_p), POINTER(c_void_p), c_void_p,
                                          POINTER(c_uint64), POINTER(c_uint64)]
     lib.gpumpi_plan_destroy.argtypes = [c_void_p]
@@ -116,6 +118,14 @@ class Plan:
 
     def launch(self, stream: int = 0):
         check(self.lib, self.lib.gpumpi_plan_launch(self.h, c_void_p(stream)), "gpumpi_plan_launch")
+
+    def set_sync(self, mode: int):
+        """0: launch-ordered forms when the calls are independent; 1: flag rounds."""
+        check(self.lib, self.lib.gpumpi_plan_set_sync(self.h, mode), "gpumpi_plan_set_sync")
+
+    @property
+    def launch_ordered(self) -> bool:
+        return bool(self.lib.gpumpi_plan_launch_ordered(self.h))
 
     def capture(self, stream: int = 0):
         check(self.lib, self.lib.gpumpi_plan_capture(self.h, c_void_p(stream)), "gpumpi_plan_capture")

@@ -195,6 +195,18 @@ int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, int threads_
                           const int* plain_threads, gpumpi_plan_t* plan);
 /* Enqueue the plan on a stream (asynchronous). */
 int gpumpi_plan_launch(gpumpi_plan_t plan, void* stream);
+/* Synchronisation of a plan's calls.  mode 0 (the default): when no call of
+ * the plan writes memory that another call reads or writes and none is a
+ * barrier (checked at creation), the batched launch runs every call in its
+ * launch-ordered form, which needs no flag round between the ranks: the
+ * inputs were complete when the launch started and the end of the launch
+ * orders the results.  A plain launch holds one call and is always
+ * launch-ordered in mode 0.  mode 1: every call synchronises its ranks with
+ * arrive/depart flags, as the device MPI_* calls do.  Drops a captured graph
+ * (capture again to replay).  No counterpart in the reference. */
+int gpumpi_plan_set_sync(gpumpi_plan_t plan, int mode);
+/* 1 when the plan's launches run the launch-ordered forms, else 0. */
+int gpumpi_plan_launch_ordered(gpumpi_plan_t plan);
 /* Capture the plan's launches once as a CUDA graph; later launches replay it. */
 int gpumpi_plan_capture(gpumpi_plan_t plan, void* stream);
 /* Host-buffer form: per-rank host->device copies of the send data, the plan,

@@ -36,11 +36,12 @@ def _rank_fold(xs, op):
 
 
 @pytest.mark.parametrize("algo", [0, 1, 2, 3])
-@pytest.mark.parametrize("form", ["plain", "batched", "graph"])
+@pytest.mark.parametrize("form", ["plain", "batched", "graph", "plain-flags", "graph-flags"])
 @pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (32, 1 << 16)])
 def test_capi_collectives(coll, form, nranks, count, algo):
     """Every schedule (algo 1-3 and the size-based choice 0) folds in rank
-    order, so each gives the host fold's bits."""
+    order, so each gives the host fold's bits, in the launch-ordered forms
+    (the calls are independent) and with flag rounds (-flags)."""
     import torch
 
     mod, lib = coll
@@ -79,8 +80,12 @@ def test_capi_collectives(coll, form, nranks, count, algo):
         # Reduce has schedules 1 and 2; Allreduce 1-3 (3: every rank pushes its
         # segment); Alltoall/Allgather 1-3 (3: bulk engine)
         d.algo = 2 if (d.op == mod.COLL_REDUCE and algo == 3) else algo
-    plan = mod.Plan(lib, descs, threads=128, batched=(form != "plain"))
-    if form == "graph":
+    plan = mod.Plan(lib, descs, threads=128, batched=not form.startswith("plain"))
+    assert plan.launch_ordered
+    if form.endswith("-flags"):
+        plan.set_sync(1)
+        assert not plan.launch_ordered
+    if form.startswith("graph"):
         plan.capture()
     for _ in range(2):
         plan.launch()
@@ -266,3 +271,46 @@ def test_plan_run_host_with_packed_host_buffers(coll):
     plan.close()
     for c in comms:
         c.close()
+
+
+@pytest.mark.parametrize("threads", [64, 256])
+def test_dependent_calls_keep_their_flag_rounds(coll, threads):
+    """A plan whose second Allreduce reads the first one's output (and whose
+    Alltoall writes a buffer the first Allreduce reads) is not launch-ordered:
+    its calls synchronise with flags, in order, and give the rank-order
+    folds of the chained calls."""
+    import torch
+
+    mod, lib = coll
+    p, n = 24, 5000
+    comm = mod.Comm(lib, p)
+    g = torch.Generator().manual_seed(99)
+    xs = [torch.rand(n, dtype=torch.float64, generator=g) * 2 - 1 for _ in range(p)]
+    d_in = [x.cuda() for x in xs]
+    d_mid = [torch.empty_like(d) for d in d_in]
+    d_out = [torch.empty_like(d) for d in d_in]
+    per = n // p
+    a2_in = [torch.rand(per * p, dtype=torch.float64, generator=g).cuda() for _ in range(p)]
+    keep = []
+    descs = [mod.make_desc(comm, mod.COLL_ALLREDUCE, "float64", n, [t.data_ptr() for t in d_in],
+                           [t.data_ptr() for t in d_mid], mod.OP_SUM, 0, keep),
+             mod.make_desc(comm, mod.COLL_ALLREDUCE, "float64", n, [t.data_ptr() for t in d_mid],
+                           [t.data_ptr() for t in d_out], mod.OP_SUM, 0, keep),
+             # writes the first call's input buffers (a write-after-read hazard)
+             mod.make_desc(comm, mod.COLL_ALLTOALL, "float64", per, [t.data_ptr() for t in a2_in],
+                           [t.data_ptr() for t in d_in], 0, 0, keep)]
+    plan = mod.Plan(lib, descs, threads=threads, batched=True)
+    assert not plan.launch_ordered
+    plan.launch()
+    torch.cuda.synchronize()
+    assert mod.status(lib) is None
+    mid = _rank_fold([x.numpy() for x in xs], "sum")
+    out = _rank_fold([mid] * p, "sum")
+    for r in range(p):
+        assert np.array_equal(d_mid[r].cpu().numpy().view(np.uint64), mid.view(np.uint64))
+        assert np.array_equal(d_out[r].cpu().numpy().view(np.uint64), out.view(np.uint64))
+        got = d_in[r].cpu().numpy()
+        for q in range(p):
+            assert np.array_equal(got[q * per:(q + 1) * per], a2_in[q].cpu().numpy()[r * per:(r + 1) * per])
+    plan.close()
+    comm.close()
