@@ -658,10 +658,7 @@ def main():
                       "steps": args.steps, "threads_per_rank": threads, "launch_ordered": bool(ordered),
                       "tuned_plain_value": round(plain_tuned_gbs, 2) if plain_tuned_gbs else None,
                       "batched_over_tuned_plain": round(kernel_gbs / plain_tuned_gbs, 2) if plain_tuned_gbs else None,
-                      "sustained": sustained,
-            "sweep": sweep,
-            "apps": apps,
-            "verified": True, "l2_resident": False})
+                      "verified": True, "l2_resident": False})
     sweep.sort(key=lambda d: d["elements_per_rank"])
 
     cpu = None
@@ -719,6 +716,9 @@ def main():
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne,
                     "form": "gpumpi_plan_run_host, the 16 communicators as 4 batched plans on 4 streams"},
+            "sustained": sustained,
+            "sweep": sweep,
+            "apps": apps,
             "verified": True,
             "verification": {"what": "every call of the timed plan after the timed region: Bcast and Alltoall "
                                      "outputs compared with their sources in full, Allreduce outputs of every "

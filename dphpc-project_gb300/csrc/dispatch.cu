@@ -69,7 +69,9 @@ __device__ __noinline__ int dispatch_all(int tid) {
             void (*body)(long, void*) = (void (*)(long, void*))c.a[0];
             void* arg = (void*)c.a[1];
             const long n = (long)c.a[2];
-            for (long i = tid; i < n; i += T) body(i, arg);
+            if (b.cl_n > 1) rc = cluster_parfor(body, arg, n, tid, T);   // the rank's helper blocks take shares
+            else
+                for (long i = tid; i < n; i += T) body(i, arg);
             break;
         }
         default: rc = MPI_ERR_INTERN; break;

@@ -91,6 +91,7 @@ size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, cha
     size_t o_sarr = c.take(sizeof(u64) * (size_t)n * 3);
     size_t o_status = c.take(sizeof(int) * 16);
     size_t o_ret = c.take(sizeof(int) * (size_t)n);
+    size_t o_cldone = c.take(sizeof(u64) * (size_t)n);
     size_t o_offs = c.take(sizeof(u64) * 4);
     size_t o_hctl = c.take(heap_ctl_bytes());
     size_t o_meta = c.take(meta_bytes * npages);
@@ -146,6 +147,7 @@ size_t host_job_layout(HostJob& hj, const gpumpi_opts& o, int n, int job_id, cha
     j.out_bytes = o.out_bytes;
     j.status = (int*)(base + o_status);
     j.retvals = (int*)(base + o_ret);
+    j.cl_done = (u64*)(base + o_cldone);
     j.err_msg = base + o_errmsg;
     // heap
     Heap& h = j.heap;
@@ -249,6 +251,8 @@ extern "C" int gpumpi_parse_args(int argc, char** argv, gpumpi_opts* o) {
                 "  --timeout-ms MS          bound of every device wait (default 60000)\n"
                 "  --out-bytes BYTES        output buffer per stream (default 16M)\n"
                 "  --max-seconds S          host wall-clock limit (default none)\n"
+                "  --blocks-per-rank C      each rank a cluster of C thread blocks (1, 2, 4, 8; default 1):\n"
+                "                           parallel loops run on all of them\n"
                 "  -v, --verbose            launch details on stderr\n");
             exit(0);
         } else if (a == "-n" || a == "--numProcs") {
@@ -280,6 +284,9 @@ extern "C" int gpumpi_parse_args(int argc, char** argv, gpumpi_opts* o) {
         } else if (a == "--max-seconds") {
             if (!next(&v)) return -2;
             o->max_seconds = atof(v.c_str());
+        } else if (a == "--blocks-per-rank") {
+            if (!next(&v)) return -2;
+            o->blocks_per_rank = atoi(v.c_str());
         } else if (a == "-v" || a == "--verbose") {
             o->verbose = 1;
         } else {
@@ -534,8 +541,14 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         set_last_error("number of ranks must be positive");
         return GPUMPI_EINVAL;
     }
+    const int C = o.blocks_per_rank > 0 ? o.blocks_per_rank : 1;
+    if (C != 1 && C != 2 && C != 4 && C != 8) {
+        set_last_error("--blocks-per-rank must be 1, 2, 4 or 8");
+        fprintf(stderr, "GPUMPI: --blocks-per-rank must be 1, 2, 4 or 8\n");
+        return GPUMPI_EINVAL;
+    }
     int max_res = 0;
-    int T = choose_threads(kernel, n, o.threads_per_rank, rank_smem_bytes(0), &max_res);
+    int T = choose_threads(kernel, n * C, o.threads_per_rank, rank_smem_bytes(0), &max_res);
     if (T == 0 || T % 32 || T < 64 || T > 1024) {
         char m[256];
         snprintf(m, sizeof(m),
@@ -547,7 +560,32 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         return GPUMPI_ENORES;
     }
     o.threads_per_rank = T;
-    const size_t smem = pick_rank_smem(kernel, T, n);
+    const size_t smem = pick_rank_smem(kernel, T, n * C);
+    if (C > 1) {
+        // every cluster (rank) must be resident at once
+        cudaLaunchConfig_t q;
+        memset(&q, 0, sizeof(q));
+        q.gridDim = dim3(n * C);
+        q.blockDim = dim3(T);
+        q.dynamicSmemBytes = smem;
+        cudaLaunchAttribute qa[1];
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = C;
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        q.attrs = qa;
+        q.numAttrs = 1;
+        int clusters = 0;
+        HCHECK(cudaOccupancyMaxActiveClusters(&clusters, kernel, &q));
+        if (clusters < n) {
+            char m[200];
+            snprintf(m, sizeof(m), "%d ranks of %d blocks cannot all be resident (at most %d clusters fit)", n, C,
+                     clusters);
+            set_last_error(m);
+            fprintf(stderr, "GPUMPI: %s\n", m);
+            return GPUMPI_ENORES;
+        }
+    }
     HCHECK(cudaDeviceSetLimit(cudaLimitStackSize, o.stack_bytes));
 
     HostJob hj;
@@ -599,10 +637,29 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     L.slot_base = 0;
     void* args[] = {&L};
     if (o.verbose)
-        fprintf(stderr, "GPUMPI: %d ranks x %d threads, job memory %.1f MiB, heap %.1f MiB\n", n, T,
-                total / 1048576.0, o.heap_bytes / 1048576.0);
+        fprintf(stderr, "GPUMPI: %d ranks x %d block(s) x %d threads, job memory %.1f MiB, heap %.1f MiB\n", n, C,
+                T, total / 1048576.0, o.heap_bytes / 1048576.0);
     const double t0 = now_s();
-    HCHECK(cudaLaunchCooperativeKernel(kernel, dim3(n), dim3(T), args, smem, st));
+    if (C == 1) {
+        HCHECK(cudaLaunchCooperativeKernel(kernel, dim3(n), dim3(T), args, smem, st));
+    } else {
+        cudaLaunchConfig_t cfg;
+        memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3(n * C);
+        cfg.blockDim = dim3(T);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[2];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        at[1].id = cudaLaunchAttributeClusterDimension;
+        at[1].val.clusterDim.x = C;
+        at[1].val.clusterDim.y = 1;
+        at[1].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 2;
+        HCHECK(cudaLaunchKernelExC(&cfg, kernel, args));
+    }
     cudaEvent_t done;
     HCHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
     HCHECK(cudaEventRecord(done, st));

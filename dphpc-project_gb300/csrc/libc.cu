@@ -396,8 +396,10 @@ static __device__ bool can_fan_out(u64 n) {
 
 __device__ void* __gpu_malloc(size_t size) { return heap_alloc(&bctx().job->heap, size); }
 
-// Parallel loop over the rank's whole thread block.  The leader hands the loop
-// to the block like an MPI call; each thread runs iterations tid, tid+T, ...;
+// Parallel loop over the rank's whole thread block (over every block of the
+// rank's cluster when the job runs ranks as clusters, see cluster.cu).  The
+// leader hands the loop to the block like an MPI call; each thread runs
+// iterations tid, tid+T, ... (tid counts the threads of the whole cluster);
 // the call returns after a block barrier, so every iteration's writes are
 // visible to the leader.  `arg` is passed to every thread, so it must point to
 // memory all threads can read (heap, globals); pointers into the leader's
@@ -989,6 +991,7 @@ __device__ clock_t __gpu_clock(void) { return (clock_t)(gtime() / 1000ull); }
 __device__ int __gpu_omp_get_max_threads(void) { return 1; }
 __device__ int __gpu_omp_get_num_threads(void) { return 1; }
 __device__ int __gpu_omp_get_thread_num(void) { return 0; }
+__device__ int __gpu_loop_block(void) { return bctx().cl_rank; }
 __device__ double __gpu_omp_get_wtime(void) { return (double)gtime() * 1e-9; }
 
 // POSIX getopt with per-rank state.

@@ -24,6 +24,10 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Lau
     using namespace gm;
     if (!program_block_begin(L)) return;
     BlockCtx& b = bctx();
+    if (b.cl_rank > 0) {   // a helper block of a cluster rank: shares of its parallel loops
+        cluster_helper_loop();
+        return;
+    }
     if (threadIdx.x == 0) {
         int rc;
         if (L.slot_base + (int)gridDim.x > __gpu_max_threads()) {
@@ -37,6 +41,7 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Lau
         } else {
             rc = __gpu_main(b.job->argc, b.job->argv);
         }
+        cluster_release();
         rank_finish(rc);
         b.call.op = OP_EXIT;
         bar_named(1, b.T);

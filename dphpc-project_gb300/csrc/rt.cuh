@@ -282,6 +282,7 @@ struct Job {
     char* err_msg;                // 256 bytes
     u64 t0_ns;                    // %globaltimer at launch
     HostCall* hcall;              // [nranks] mapped host memory, or null: no host service
+    u64* cl_done;                 // [nranks] loop shares finished by a rank's helper blocks
 };
 
 // Device -> host calls (file I/O of converted programs).  One slot per rank in
@@ -521,6 +522,23 @@ struct BlockCtx {
     const void* sc_handle;
     const int* sc_members;
     int sc_ctx, sc_me, sc_size;
+    // A rank may be a cluster of cl_n thread blocks (cl_n = 1: one block).
+    // Block cl_rank 0 runs the program; the others ("helper blocks") take
+    // shares of its parallel loops.  The leader block writes a command into
+    // a helper block's cl_cmd through distributed shared memory and arrives
+    // on the helper's cl_go barrier; helpers report completion through the
+    // job's cl_done counter of the rank in global memory, so that no helper
+    // ever touches the leader block's shared memory.
+    int cl_n;
+    int cl_rank;
+    int cl_released;              // leader: the helpers were told to exit
+    u32 cl_phase;                 // leader: loops handed out; helper: commands taken
+    u64 cl_go;                    // helper: mbarrier (count 1), arrived on by the leader block
+    struct ClusterCmd {
+        int op;                   // OP_PARFOR or OP_EXIT
+        int pad;
+        u64 a[3];                 // body, argument, iterations
+    } cl_cmd;
 };
 
 static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");
@@ -680,6 +698,12 @@ __device__ int comm_split_block(MPI_Comm_impl* parent, int color, int key, MPI_C
 __device__ void* heap_alloc(Heap* h, u64 bytes);
 __device__ void heap_free(Heap* h, void* p);
 __device__ u64 heap_usable_size(Heap* h, void* p);
+
+// cluster ranks (csrc/cluster.cu)
+__device__ void cluster_setup(int tid);                       // every block of a cluster, at start
+__device__ int cluster_parfor(void (*body)(long, void*), void* arg, long n, int tid, int T);
+__device__ void cluster_release();                            // leader block: helpers may exit
+__device__ void cluster_helper_loop();                        // helper blocks
 
 // rank lifecycle
 __device__ void rank_init(int tid, int T);

@@ -444,6 +444,7 @@ __device__ void rank_exit_now(int status) {
         atomicCAS(&j->status[6], 0, status);
         job_fail(j, b.rank, GPUMPI_ERR_ABORTED, "a rank called exit() or abort() with nonzero status");
     }
+    cluster_release();
     rank_finish(status);
     if (b.leader_mode && !b.in_call) {
         b.call.op = OP_EXIT;
@@ -468,7 +469,11 @@ namespace gm {
 // initialise the rank.  Returns false for idle slots.
 __device__ bool program_block_begin(const Launch& L) {
     BlockCtx& b = bctx();
-    const int slot = blockIdx.x;
+    // a rank is one cluster: C consecutive blocks (C = 1 without a cluster launch)
+    u32 C, crank;
+    asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(C));
+    asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(crank));
+    const int slot = (int)(blockIdx.x / C);
     if (threadIdx.x == 0) {
         const int jid = slot < L.nslots ? L.slot_job[slot] : -1;
         if (jid < 0) {
@@ -484,11 +489,18 @@ __device__ bool program_block_begin(const Launch& L) {
             b.bulk_broken = 0;
             b.lazy_n = 0;
             b.call.op = -1;
+            b.cl_n = (int)C;
+            b.cl_rank = (int)crank;
+            b.cl_released = 0;
+            b.cl_phase = 0;
+            b.cl_cmd.op = -1;
+            if (crank > 0) b.leader_mode = 0;   // a helper block of a cluster rank
         }
     }
     __syncthreads();
     if (!b.job) return false;
-    rank_init((int)threadIdx.x, (int)blockDim.x);
+    if (crank == 0) rank_init((int)threadIdx.x, (int)blockDim.x);
+    cluster_setup((int)threadIdx.x);
     return true;
 }
 

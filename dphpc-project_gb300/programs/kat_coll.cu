@@ -12,6 +12,7 @@
 #include "stdlib.h.cuh"
 #include "string.h.cuh"
 #include "stdint.h.cuh"
+#include "omp.h.cuh"
 
 __device__ int reduce_prod(int rank, int size) {
     int16_t buf[14], out[14], expect[14];
@@ -359,6 +360,88 @@ __device__ int groups_cart(int rank, int size) {
     return ok;
 }
 
+// User-defined operator that is not commutative: inout = inout * 31 + in (mod
+// 2^32).  Folded in rank order (acc = x_0; acc = op(x_q, acc)) the result is
+// the Horner value of x_0, x_1, ..., x_{P-1}, so any other order shows.
+__device__ void horner_op(void* in, void* inout, int* len, MPI_Datatype* dt) {
+    const unsigned* a = (const unsigned*)in;
+    unsigned* b = (unsigned*)inout;
+    for (int i = 0; i < *len; i++) b[i] = b[i] * 31u + a[i];
+}
+
+__device__ unsigned user_x(int q, long i) { return (unsigned)(q * 2654435761u) ^ (unsigned)(i * 40503u + 7u); }
+
+__device__ int user_op(int rank, int size) {
+    MPI_Op op;
+    int ok = 1;
+    if (MPI_Op_create(horner_op, 0, &op) != MPI_SUCCESS) return 0;
+    const int counts[3] = {1, 1000, 70001};
+    for (int k = 0; k < 3; k++) {
+        const int n = counts[k];
+        unsigned* x = (unsigned*)malloc(sizeof(unsigned) * n);
+        unsigned* r = (unsigned*)malloc(sizeof(unsigned) * n);
+        unsigned* a = (unsigned*)malloc(sizeof(unsigned) * n);
+        for (long i = 0; i < n; i++) {
+            x[i] = user_x(rank, i);
+            r[i] = 0;
+            a[i] = 0;
+        }
+        MPI_Reduce(x, r, n, MPI_UNSIGNED, op, 0, MPI_COMM_WORLD);
+        MPI_Allreduce(x, a, n, MPI_UNSIGNED, op, MPI_COMM_WORLD);
+        for (long i = 0; i < n; i++) {
+            unsigned acc = user_x(0, i);
+            for (int q = 1; q < size; q++) acc = acc * 31u + user_x(q, i);
+            if (a[i] != acc) ok = 0;
+            if (rank == 0 && r[i] != acc) ok = 0;
+        }
+        free(x);
+        free(r);
+        free(a);
+    }
+    MPI_Op_free(&op);
+    if (op != MPI_OP_NULL) ok = 0;
+    return ok;
+}
+
+// Parallel loop: every iteration runs once; with a rank made of several
+// thread blocks (a cluster), iterations run on all of them.
+struct loop_arg {
+    long* out;
+    int* blk;
+};
+
+__device__ void loop_body(long i, void* p) {
+    struct loop_arg* a = (struct loop_arg*)p;
+    a->out[i] += i * 3 + 1;
+    a->blk[i] = gpumpi_loop_block();
+}
+
+__device__ int parfor(int rank, int size) {
+    const long n = 200003;
+    struct loop_arg* a = (struct loop_arg*)malloc(sizeof(struct loop_arg));
+    a->out = (long*)malloc(sizeof(long) * n);
+    a->blk = (int*)malloc(sizeof(int) * n);
+    for (long i = 0; i < n; i++) {
+        a->out[i] = rank;
+        a->blk[i] = -1;
+    }
+    gpumpi_parallel_for(n, loop_body, a);
+    int ok = 1;
+    int seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long i = 0; i < n; i++) {
+        if (a->out[i] != rank + i * 3 + 1) ok = 0;
+        if (a->blk[i] < 0 || a->blk[i] >= 8) ok = 0;
+        else seen[a->blk[i]] = 1;
+    }
+    int blocks = 0;
+    for (int k = 0; k < 8; k++) blocks += seen[k];
+    printf("parfor rank %d blocks %d\n", rank, blocks);
+    free(a->out);
+    free(a->blk);
+    free(a);
+    return ok;
+}
+
 __device__ int __gpu_main(int argc, char** argv) {
     int rank, size, ok = 0;
     MPI_Init(&argc, &argv);
@@ -375,6 +458,8 @@ __device__ int __gpu_main(int argc, char** argv) {
     else if (!strcmp(s, "comm_split")) ok = comm_split(rank, size);
     else if (!strcmp(s, "extras")) ok = extras(rank, size);
     else if (!strcmp(s, "groups_cart")) ok = groups_cart(rank, size);
+    else if (!strcmp(s, "user_op")) ok = user_op(rank, size);
+    else if (!strcmp(s, "parfor")) ok = parfor(rank, size);
     printf("%s rank %d ok %d\n", s, rank, ok);
     MPI_Finalize();
     return 0;

@@ -52,6 +52,8 @@ typedef struct gpumpi_opts {
     size_t out_bytes;        /* stdout and stderr buffer size per job (default 16 MiB) */
     double max_seconds;      /* host wall-clock limit of the whole run, 0 = none */
     int verbose;             /* print GPUMPI: launch lines on stderr */
+    int blocks_per_rank;     /* --blocks-per-rank: each rank a cluster of this many thread
+                                blocks (1, 2, 4, 8; 0 = 1); parallel loops span all of them */
 } gpumpi_opts;
 
 /* Exported by every program library: parse "---gpumpi" options from argv,

@@ -153,6 +153,9 @@ __device__ void __gpu_parallel_for(long n, __gpu_loop_body body, void* arg);
 __device__ int __gpu_omp_get_max_threads(void);
 __device__ int __gpu_omp_get_num_threads(void);
 __device__ int __gpu_omp_get_thread_num(void);
+// Inside a parallel loop body: the index of the thread block running it within
+// the rank (0 unless the job runs each rank as a cluster of blocks).
+__device__ int __gpu_loop_block(void);
 __device__ double __gpu_omp_get_wtime(void);
 
 // assert: records the failure for the job and ends the rank

@@ -5,6 +5,7 @@
 #define omp_get_thread_num __gpu_omp_get_thread_num
 #define omp_get_wtime __gpu_omp_get_wtime
 #define gpumpi_parallel_for __gpu_parallel_for
+#define gpumpi_loop_block __gpu_loop_block
 // 64-bit integer add that concurrent loop iterations may apply to the same
 // word (exact, so its result does not depend on their order).
 __device__ inline void gpumpi_atomic_add_i64(long long* p, long long v) {

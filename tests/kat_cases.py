@@ -35,6 +35,10 @@ KAT_CASES = [
     ("kat_coll", "extras", 16),
     ("kat_coll", "groups_cart", 6),
     ("kat_coll", "groups_cart", 12),
+    ("kat_coll", "user_op", 1),
+    ("kat_coll", "user_op", 6),
+    ("kat_coll", "user_op", 33),
+    ("kat_coll", "parfor", 4),
     ("kat_global", None, 4),
 ]
 

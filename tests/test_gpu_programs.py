@@ -137,3 +137,55 @@ def test_gpu_pi_matches_reference_program(gpu_built, n, ranks, line):
     g = gpu_built.run_program("pi", [str(n)], nranks=ranks, extra=GPU_OPTS, timeout=180)
     assert g.returncode == 0, g.stderr
     assert g.lines("pi is approximately") == [line]
+
+
+# ---------------------------------------------------------------- ranks as clusters of thread blocks
+
+CLUSTER_KAT = [c for c in KAT_CASES if c[0] in ("kat_p2p", "kat_coll")]
+
+
+@pytest.mark.parametrize("blocks", [2, 4])
+@pytest.mark.parametrize("prog,scenario,nranks", CLUSTER_KAT)
+def test_gpu_known_answers_with_cluster_ranks(gpu_built, prog, scenario, nranks, blocks):
+    """Every known-answer scenario with each rank launched as a cluster of
+    2 or 4 thread blocks (the helper blocks take shares of parallel loops)."""
+    args = [scenario] if scenario else []
+    res = gpu_built.run_program(prog, args, nranks=nranks, extra=GPU_OPTS + ["--blocks-per-rank", str(blocks)],
+                                timeout=180)
+    check_all_ok(res, scenario, nranks)
+
+
+@pytest.mark.parametrize("blocks", [1, 2, 4, 8])
+def test_gpu_parallel_loop_spans_the_cluster(gpu_built, blocks):
+    """A parallel loop of a rank made of `blocks` thread blocks runs every
+    iteration exactly once and runs iterations on all of the blocks."""
+    res = gpu_built.run_program("kat_coll", ["parfor"], nranks=4,
+                                extra=GPU_OPTS + ["--blocks-per-rank", str(blocks)], timeout=180)
+    check_all_ok(res, "parfor", 4)
+    assert sorted(res.lines("parfor rank")) == [f"parfor rank {r} blocks {blocks}" for r in range(4)]
+
+
+def test_gpu_cluster_ranks_reject_bad_sizes(gpu_built):
+    res = gpu_built.run_program("kat_coll", ["parfor"], nranks=2, extra=GPU_OPTS + ["--blocks-per-rank", "3"],
+                                timeout=60)
+    assert res.returncode != 0
+    assert "blocks-per-rank" in res.stderr
+
+
+@pytest.mark.parametrize("prog,args,ranks,heap,blocks", [
+    ("pic", ["10", "64", "32", "20", "5"], 16, "1G", 2),
+    ("pic", ["50", "256", "128", "125", "10"], 64, "4G", 2),
+    ("is_sort", ["23", "10"], 64, "2G", 2),
+    ("is_sort", ["14", "3"], 7, "1G", 4),
+])
+def test_gpu_apps_with_cluster_ranks_match_oracle(gpu_built, prog, args, ranks, heap, blocks):
+    """PIC and the IS-like sort with every rank a cluster of thread blocks:
+    the printed results (energies, checksums) equal the host MPI run's."""
+    g = gpu_built.run_program(prog, args, nranks=ranks,
+                              extra=GPU_OPTS + ["-p", heap, "--blocks-per-rank", str(blocks)], timeout=600)
+    c = run_oracle(prog, args, nranks=ranks, timeout=600)
+    assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
+    assert c.returncode == 0, c.stderr[-2000:]
+    key = "pic " if prog == "pic" else "is "
+    strip = lambda lines: [ln for ln in lines if "-time" not in ln]
+    assert strip(g.lines(key)) == strip(c.lines(key))
