@@ -359,6 +359,7 @@ def app_runs(host, timeout: float = 600.0) -> dict:
     import importlib.util
     spec = importlib.util.spec_from_file_location("hostmpi_run", os.path.join(ROOT, "oracle", "hostmpi_run.py"))
     oracle = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = oracle
     spec.loader.exec_module(oracle)
     out = {}
     for name, prog, pargs, ranks, extra, pat in APPS:

@@ -20,17 +20,14 @@ __device__ bool program_block_begin(const Launch& L);
 // (include/gpumpi/global_vars.cuh); it must alias the runtime's block context.
 extern __shared__ __align__(16) char __gpumpi_dsmem[];
 
-extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Launch L) {
+// Run the rank set up in this block: thread 0 runs the program, the other
+// threads execute its MPI calls.  Returns when the rank has finished.
+static __device__ void run_rank() {
     using namespace gm;
-    if (!program_block_begin(L)) return;
     BlockCtx& b = bctx();
-    if (b.cl_rank > 0) {   // a helper block of a cluster rank: shares of its parallel loops
-        cluster_helper_loop();
-        return;
-    }
     if (threadIdx.x == 0) {
         int rc;
-        if (L.slot_base + (int)gridDim.x > __gpu_max_threads()) {
+        if (b.slot >= __gpu_max_threads()) {
             job_fail(b.job, b.rank, MPI_ERR_INTERN,
                      "rank slots exceed the per-rank global arrays the program was compiled with "
                      "(GPU_MPI_MAX_RANKS)");
@@ -50,15 +47,51 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Lau
     }
 }
 
+extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Launch L) {
+    using namespace gm;
+    if (!program_block_begin(L)) return;
+    if (bctx().cl_rank > 0) {   // a helper block of a cluster rank: shares of its parallel loops
+        cluster_helper_loop();
+        return;
+    }
+    run_rank();
+}
+
+// Serving runtime (server.cu): blocks 0..nworkers-1 are rank slots that run
+// one rank of an admitted job after another; block nworkers is the admin
+// block.  A rank that ends with exit() retires its leader thread, and with it
+// the block: its slot is reported lost and receives no further ranks.
+extern "C" __global__ void __launch_bounds__(1024) gpumpi_server_kernel(gm::ServerArgs A) {
+    using namespace gm;
+    if ((int)blockIdx.x == A.nworkers) {
+        server_admin(A);
+        return;
+    }
+    const int w = (int)blockIdx.x;
+    u64 seen = 0;
+    Job* job;
+    int rank;
+    while (server_take(A, w, &seen, &job, &rank)) {
+        rank_block_setup(job, rank, A.slot_base + w);
+        run_rank();
+        if (threadIdx.x != 0 && bctx().priv->exited) {
+            // the leader thread has left the kernel (exit(), abort(), a failed assert)
+            if (threadIdx.x == 1) {
+                A.lost[w] = 1;
+                __threadfence();
+            }
+            return;
+        }
+        __syncthreads();
+    }
+}
+
 extern "C" int gpumpi_main(int argc, char** argv) {
     for (int i = 1; i < argc; i++) {
         if (strcmp(argv[i], "---gpumpi") != 0) continue;
         for (int k = i + 1; k < argc; k++)
             if (strcmp(argv[k], "--serve") == 0) {
-                // jobs run as concurrent kernels on their own streams: give them
-                // enough hardware queues (read when the CUDA context is created)
-                setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
-                return gpumpi_serve_main((const void*)gpumpi_program_kernel, argc, argv);
+                return gpumpi_serve_main((const void*)gpumpi_server_kernel, argc, argv);
             }
         break;
     }

@@ -313,6 +313,49 @@ struct alignas(64) HostCall {
 };
 static_assert(offsetof(HostCall, data) % 16 == 0, "HostCall data alignment");
 
+// ---------------------------------------------------------------- serving runtime
+// A server is one persistent cooperative launch: `nworkers` worker blocks,
+// each a rank slot that runs one rank of an admitted job after another, and
+// one admin block.  The host posts admission records into a ring in pinned
+// host memory mapped into the device; the admin block (the only reader of
+// that memory) hands each admitted job's ranks to their worker blocks through
+// device memory, watches the running jobs and posts the ticket of each
+// finished job into the completion ring.
+constexpr int SERVE_RING = 256;       // records of each ring
+constexpr int SERVE_MAX_JOBS = 256;   // jobs running at once
+struct AdmitRec {
+    Job* job;                         // the job's device record (in its memory, initialised)
+    int slot_base;                    // ranks r run on worker blocks slot_base + r
+    int nranks;
+    u64 ticket;
+};
+struct ServeRing {
+    u64 sub_head;                     // admission records posted (host writes)
+    u64 pad0[15];
+    AdmitRec sub[SERVE_RING];
+    u64 done_head;                    // completion records posted (device writes)
+    u64 pad1[15];
+    u64 done[SERVE_RING];             // tickets of finished jobs
+    int stop;                         // host: end once every admitted job has finished
+    int kill;                         // host: end now (idle workers leave)
+};
+struct ServeActive {
+    Job* job;
+    int nranks;
+    int slot_base;
+    u64 ticket;
+};
+struct ServerArgs {
+    ServeRing* ring;                  // device address of the mapped ring
+    u64* assign_seq;                  // [nworkers] assignment counter; ~0 = stop
+    Job** assign_job;                 // [nworkers]
+    int* assign_rank;                 // [nworkers]
+    int* lost;                        // [nworkers] 1: the block left (a rank called exit())
+    ServeActive* active;              // [SERVE_MAX_JOBS] admin block's table
+    int nworkers;
+    int slot_base;                    // rank slot of worker block 0
+};
+
 // Where a thread block finds its job: slot -> (job, rank).
 struct Launch {
     Job* jobs;
@@ -704,6 +747,11 @@ __device__ void cluster_setup(int tid);                       // every block of 
 __device__ int cluster_parfor(void (*body)(long, void*), void* arg, long n, int tid, int T);
 __device__ void cluster_release();                            // leader block: helpers may exit
 __device__ void cluster_helper_loop();                        // helper blocks
+
+// serving runtime (csrc/server.cu)
+__device__ void server_admin(const ServerArgs& A);
+__device__ bool server_take(const ServerArgs& A, int w, u64* seen, Job** job, int* rank);
+__device__ void rank_block_setup(Job* job, int rank, int slot);   // every thread; one-block rank
 
 // rank lifecycle
 __device__ void rank_init(int tid, int T);

@@ -465,6 +465,35 @@ __device__ void rank_finish(int rc) {
 
 namespace gm {
 
+// Thread 0: the block context of rank `rank` of `job` in rank slot `slot`,
+// block `crank` of a rank made of C blocks.
+static __device__ void block_ctx_init(Job* job, int rank, int slot, u32 C, u32 crank) {
+    BlockCtx& b = bctx();
+    b.job = job;
+    b.rank = rank;
+    b.priv = &job->priv[rank];
+    b.slot = slot;
+    b.T = (int)blockDim.x;
+    b.leader_mode = 1;
+    b.in_call = 0;
+    b.bulk_broken = 0;
+    b.lazy_n = 0;
+    b.call.op = -1;
+    b.cl_n = (int)C;
+    b.cl_rank = (int)crank;
+    b.cl_released = 0;
+    b.cl_phase = 0;
+    b.cl_cmd.op = -1;
+    if (crank > 0) b.leader_mode = 0;   // a helper block of a cluster rank
+}
+
+// Worker blocks of a server: one rank of one block, set up and initialised.
+__device__ void rank_block_setup(Job* job, int rank, int slot) {
+    if (threadIdx.x == 0) block_ctx_init(job, rank, slot, 1, 0);
+    __syncthreads();
+    rank_init((int)threadIdx.x, (int)blockDim.x);
+}
+
 // Block set-up for program kernels: find this slot's job and rank, then
 // initialise the rank.  Returns false for idle slots.
 __device__ bool program_block_begin(const Launch& L) {
@@ -479,22 +508,7 @@ __device__ bool program_block_begin(const Launch& L) {
         if (jid < 0) {
             b.job = nullptr;
         } else {
-            b.job = &L.jobs[jid];
-            b.rank = L.slot_rank[slot];
-            b.priv = &b.job->priv[b.rank];
-            b.slot = L.slot_base + slot;
-            b.T = (int)blockDim.x;
-            b.leader_mode = 1;
-            b.in_call = 0;
-            b.bulk_broken = 0;
-            b.lazy_n = 0;
-            b.call.op = -1;
-            b.cl_n = (int)C;
-            b.cl_rank = (int)crank;
-            b.cl_released = 0;
-            b.cl_phase = 0;
-            b.cl_cmd.op = -1;
-            if (crank > 0) b.leader_mode = 0;   // a helper block of a cluster rank
+            block_ctx_init(&L.jobs[jid], L.slot_rank[slot], L.slot_base + slot, C, crank);
         }
     }
     __syncthreads();
@@ -503,5 +517,6 @@ __device__ bool program_block_begin(const Launch& L) {
     cluster_setup((int)threadIdx.x);
     return true;
 }
+
 
 }  // namespace gm

@@ -37,6 +37,7 @@ extern "C" {
 #define GPUMPI_ECUDA 1002       /* a CUDA runtime call failed */
 #define GPUMPI_ENORES 1003      /* ranks cannot all be resident on the GPU at once */
 #define GPUMPI_EJOB 1004        /* the device job reported an error (see gpumpi_last_error) */
+#define GPUMPI_EAGAIN 1005      /* gpumpi_poll: the job has not finished yet */
 
 /* ---- launcher (section 1) ---- */
 
@@ -105,18 +106,44 @@ typedef struct gpumpi_job_result {
     char* err;               /* its stderr text and launcher diagnostics; gpumpi_free */
 } gpumpi_job_result;
 
-/* Run every job to completion.  A job is admitted once it has arrived, its
- * job memory fits in a free range of the pool and a contiguous range of rank
- * slots is free (running ranks never exceed what the GPU holds at once); each
- * admitted job is a cooperative launch of program_kernel on its own stream.
- * No counterpart in the reference, which ran one program per process
- * (gpu_libs/gpu_main/main.cu:163-321).  Returns 0, GPUMPI_EJOB when a job
- * failed (see its result), or an error code. */
-int gpumpi_serve(const void* program_kernel, const gpumpi_job_spec* jobs, int njobs,
+/* Run every job to completion on a server (below): each job is submitted at
+ * its arrival time and admitted once its job memory fits in a free range of
+ * the pool and a contiguous range of idle rank slots is free.  server_kernel
+ * is the program's gpumpi_server_kernel.  No counterpart in the reference,
+ * which ran one program per process (gpu_libs/gpu_main/main.cu:163-321).
+ * Returns 0, GPUMPI_EJOB when a job failed (see its result), or an error code. */
+int gpumpi_serve(const void* server_kernel, const gpumpi_job_spec* jobs, int njobs,
                  const gpumpi_serve_opts* opts, gpumpi_job_result* results);
 
+/* Online serving.  gpumpi_server_start launches server_kernel (the program's
+ * gpumpi_server_kernel) once, as one persistent cooperative launch of worker
+ * blocks (rank slots) and an admin block, and starts a host thread that
+ * admits submitted jobs as their HBM footprint and rank slots free up; jobs
+ * run side by side, and a finished job's slots and memory go to the next.
+ * The admission and completion records travel through a ring in pinned host
+ * memory.  No counterpart in the reference, which ran one program per
+ * process (gpu_libs/gpu_main/main.cu:163-321) and whose device->host queue
+ * went unused (gpu_libs/gpu_libc/cuda_mpi.cuh:392-435). */
+typedef struct gpumpi_server_s* gpumpi_server_t;
+int gpumpi_server_start(const void* server_kernel, const gpumpi_serve_opts* opts, gpumpi_server_t* server);
+/* Queue a job (its argv strings are copied); returns at once with its id.
+ * submit_s is ignored: the job arrives now.  Safe to call from any thread. */
+int gpumpi_submit(gpumpi_server_t server, const gpumpi_job_spec* job, long long* job_id);
+/* The result of a job: waits up to wait_ms (-1: until it has finished, 0:
+ * not at all).  Returns 0 and fills *result (times in seconds since the
+ * server started; release the texts with gpumpi_free), or GPUMPI_EAGAIN while
+ * the job runs or waits.  Each result is returned once. */
+int gpumpi_poll(gpumpi_server_t server, long long job_id, int wait_ms, gpumpi_job_result* result);
+/* Wait until every submitted job has finished, end the persistent launch and
+ * release the server (results not polled are discarded). */
+int gpumpi_server_stop(gpumpi_server_t server);
+
 /* Command-line form, used by gpumpi_main when "--serve JOBFILE" follows
- * "---gpumpi": one job per line, "<ranks> <arrival-ms> [arguments...]". */
+ * "---gpumpi": one job per line, "<ranks> <arrival-ms> [arguments...]";
+ * "--serve -" reads such lines from standard input and submits each job the
+ * moment its line arrives (the arrival time is then ignored), printing each
+ * job's output as it finishes.  program_kernel is the program's
+ * gpumpi_server_kernel. */
 int gpumpi_serve_main(const void* program_kernel, int argc, char** argv);
 
 /* Release memory returned by the runtime (gpumpi_job_result texts). */
