@@ -296,6 +296,7 @@ def sweep_point(coll, lib, torch, lg: int, stream, peak: float, tune_reps: int, 
     pdescs = [type(d).from_buffer_copy(d) for d in descs]
     for d, a in zip(pdescs, palg):
         d.algo = a
+        d.sync = 0
     plain = coll.Plan(lib, pdescs, threads=threads, batched=False, plain_threads=pth)
     if sync_mode:
         plain.set_sync(sync_mode)
@@ -313,7 +314,8 @@ def sweep_point(coll, lib, torch, lg: int, stream, peak: float, tune_reps: int, 
     torch.cuda.empty_cache()
     return {"elements_per_rank": n, "value": round(gbs, 2), "unit": "GB/s", "frac": round(gbs / peak, 4),
             "us_per_step": round(per_step * 1e6, 2), "steps": steps, "threads_per_rank": threads,
-            "launch_ordered": bool(ordered), "tuned_plain_value": round(pgbs, 2),
+            "launch_ordered": bool(ordered), "flag_rounds_calls": sum(1 for d in descs if d.sync),
+            "tuned_plain_value": round(pgbs, 2),
             "batched_over_tuned_plain": round(gbs / pgbs, 2), "verified": True,
             "l2_resident": nbytes < 120e6}
 
@@ -323,7 +325,11 @@ def sweep_point(coll, lib, torch, lg: int, stream, peak: float, tune_reps: int, 
 # run.  (name, program, arguments, ranks, GPU launcher options, time pattern)
 APPS = [
     ("pi_1e7_8ranks", "pi", ["10000000"], 8, [], r"wall clock time = ([0-9.]+)"),
+    ("pi_1e7_8ranks_parallel_runs_4_blocks_per_rank", "pi", ["10000000", "4096"], 8, ["--blocks-per-rank", "4"],
+     r"wall clock time = ([0-9.]+)"),
     ("p2p_pair_8B_blocking", "p2p_sweep", ["pairs", "block", "3", "3", "2000"], 2, [],
+     r"p2p-time bytes \d+ seconds ([0-9.]+)"),
+    ("p2p_pair_8B_blocking_one_cluster", "p2p_sweep", ["pairs", "block", "3", "3", "2000"], 2, ["--one-cluster"],
      r"p2p-time bytes \d+ seconds ([0-9.]+)"),
     ("p2p_pair_1MiB_nonblocking", "p2p_sweep", ["pairs", "nb", "20", "20", "200"], 2, [],
      r"p2p-time bytes \d+ seconds ([0-9.]+)"),
@@ -333,6 +339,12 @@ APPS = [
      r"p2p-time bytes \d+ seconds ([0-9.]+)"),
     ("is_like_sort_2e23_64ranks", "is_sort", ["23", "10"], 64, ["-p", "2G"], r"is-time seconds ([0-9.]+)"),
     ("pic_64ranks_50cycles", "pic", ["50"], 64, ["-p", "4G"], r"pic-time seconds ([0-9.]+)"),
+    ("pic_64ranks_50cycles_2_blocks_per_rank", "pic", ["50"], 64, ["-p", "4G", "--blocks-per-rank", "2"],
+     r"pic-time seconds ([0-9.]+)"),
+    ("pic_64ranks_50cycles_4_blocks_per_rank", "pic", ["50"], 64, ["-p", "4G", "--blocks-per-rank", "4"],
+     r"pic-time seconds ([0-9.]+)"),
+    ("is_like_sort_2e23_64ranks_2_blocks_per_rank", "is_sort", ["23", "10"], 64, ["-p", "2G", "--blocks-per-rank", "2"],
+     r"is-time seconds ([0-9.]+)"),
 ]
 TIME_LINE = re.compile(r"^(wall clock time|p2p-time|is-time|pic-time)")
 
@@ -513,6 +525,7 @@ def main():
             algos.setdefault(names[d.op], {}).setdefault(str(d.algo), 0)
             algos[names[d.op]][str(d.algo)] += 1
         tuning = {"batched_threads": threads, "algo_counts": algos, "seconds": round(tune_s, 2),
+                  "flag_rounds_calls": sum(1 for d in descs if d.sync),
                   "plain_threads_counts": {str(t): plain_threads.count(t) for t in sorted(set(plain_threads))}}
         plan = coll.Plan(lib, descs, threads=threads, batched=True)
         # the tuner ran the calls on these buffers: give every input (and the
@@ -582,6 +595,7 @@ def main():
         pdescs = [type(d).from_buffer_copy(d) for d in descs]
         for d, a in zip(pdescs, plain_algos):
             d.algo = a
+            d.sync = 0
         plain = coll.Plan(lib, pdescs, threads=threads, batched=False, plain_threads=plain_threads)
         if args.sync_mode:
             plain.set_sync(args.sync_mode)

@@ -31,7 +31,7 @@ struct DevDesc {
     int comm;       // index into the plan's communicator table
     int esize;
     int algo;
-    int pad;
+    int sync;       // 1: flag rounds even when the launch is launch-ordered
     void** sbufs;   // [P] device array
     void** rbufs;   // [P]
     const Pub* pub; // [P] buffer table of the launch-ordered forms (nullptr: none)
@@ -68,7 +68,7 @@ static __device__ int run_desc(const DevDesc& d, MPI_Comm_impl* comm, int P, int
     a.ufn = nullptr;
     const void* sb = d.sbufs ? ldcg(&d.sbufs[rank]) : nullptr;
     void* rb = d.rbufs ? ldcg(&d.rbufs[rank]) : nullptr;
-    if (ordered && d.pub) {
+    if (ordered && d.pub && !d.sync) {
         a.sbuf = sb;
         a.rbuf = rb;
         switch (d.op) {
@@ -136,6 +136,10 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_plan_kernel(PlanArgs A
         b.bulk_broken = 0;
         b.lazy_n = 0;
         b.sc_handle = nullptr;
+        b.mb_cluster = 0;
+        b.mb_local = nullptr;
+        b.cl_n = 1;
+        b.cl_rank = 0;
     }
     __syncthreads();
     MPI_Comm_impl* comm = &A.comms[c].handles[rank];
@@ -466,6 +470,7 @@ extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, i
         x.comm = cidx[i];
         x.esize = esize_of(d.dtype);
         x.algo = d.algo;
+        x.sync = d.sync ? 1 : 0;
         x.sbufs = (void**)(base + off_ptr + sizeof(void*) * pk);
         for (int r = 0; r < P; r++) hp[pk++] = d.sendbufs ? d.sendbufs[r] : nullptr;
         x.rbufs = (void**)(base + off_ptr + sizeof(void*) * pk);

@@ -25,6 +25,7 @@ namespace gm {
 constexpr u64 REDUCE_ROOT_ONLY_BYTES = 64 * 1024;     // total input bytes
 constexpr u64 ALLREDUCE_DIRECT_BYTES = 16 * 1024;     // per-rank bytes
 constexpr u64 WARP_COPY_BYTES = 16 * 1024;            // per-block copies below this go warp-parallel
+constexpr u64 TINY_BLOCK_BYTES = 128;                 // ... and below this one block per thread
 
 // Start a collective: thread 0 bumps the communicator's sequence number and
 // publishes a view of the communicator to the block (bctx().cv).
@@ -81,7 +82,8 @@ static __device__ __forceinline__ u64 seg_len(u64 n, int P, int es) {
 // block through the bulk engine in one pipeline while the other threads wait,
 // then all threads copy unaligned blocks and sub-16-byte tails; mode 0: mode 3
 // for blocks of BULK_SEG_MIN and more when the launch has a staging area,
-// else mode 1 for blocks of WARP_COPY_BYTES and more, else mode 2.
+// else mode 1 for blocks of WARP_COPY_BYTES and more, else mode 2.  Modes 0
+// and 2 copy blocks of at most TINY_BLOCK_BYTES one per thread.
 template <class F>
 static __device__ void multi_copy(int nb, int first, u64 avg_bytes, F f, int tid, int T, int mode = 0) {
     const bool staging = bulk_stage_bytes() >= 8192;
@@ -111,6 +113,31 @@ static __device__ void multi_copy(int nb, int first, u64 avg_bytes, F f, int tid
                 if (n16 < n) warp_copy((char*)d + n16, (const char*)s + n16, n - n16, lane);
             } else {
                 warp_copy(d, s, n, lane);
+            }
+        }
+        bsync();
+        return;
+    }
+    if ((mode == 0 || mode == 2) && avg_bytes <= TINY_BLOCK_BYTES) {
+        // tiny blocks: one block per thread, all of them in flight at once
+        // (a warp per block would wait one round trip per block)
+        for (int k = tid; k < nb; k += T) {
+            const void* s;
+            void* d;
+            u64 n;
+            if (!f((first + k) % nb, &s, &d, &n)) continue;
+            const char* sc = (const char*)s;
+            char* dc = (char*)d;
+            if ((((uintptr_t)sc | (uintptr_t)dc) & 15) == 0) {
+                u64 i = 0;
+                for (; i + 16 <= n; i += 16) *(uint4*)(dc + i) = __ldcg((const uint4*)(sc + i));
+                for (; i < n; i++) dc[i] = __ldcg(sc + i);
+            } else if ((((uintptr_t)sc | (uintptr_t)dc) & 7) == 0) {
+                u64 i = 0;
+                for (; i + 8 <= n; i += 8) *(u64*)(dc + i) = __ldcg((const u64*)(sc + i));
+                for (; i < n; i++) dc[i] = __ldcg(sc + i);
+            } else {
+                for (u64 i = 0; i < n; i++) dc[i] = __ldcg(sc + i);
             }
         }
         bsync();

@@ -253,6 +253,8 @@ extern "C" int gpumpi_parse_args(int argc, char** argv, gpumpi_opts* o) {
                 "  --max-seconds S          host wall-clock limit (default none)\n"
                 "  --blocks-per-rank C      each rank a cluster of C thread blocks (1, 2, 4, 8; default 1):\n"
                 "                           parallel loops run on all of them\n"
+                "  --one-cluster            all ranks (at most 16) in one thread-block cluster: their\n"
+                "                           mailboxes live in distributed shared memory\n"
                 "  -v, --verbose            launch details on stderr\n");
             exit(0);
         } else if (a == "-n" || a == "--numProcs") {
@@ -287,6 +289,8 @@ extern "C" int gpumpi_parse_args(int argc, char** argv, gpumpi_opts* o) {
         } else if (a == "--blocks-per-rank") {
             if (!next(&v)) return -2;
             o->blocks_per_rank = atoi(v.c_str());
+        } else if (a == "--one-cluster") {
+            o->one_cluster = 1;
         } else if (a == "-v" || a == "--verbose") {
             o->verbose = 1;
         } else {
@@ -547,6 +551,12 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         fprintf(stderr, "GPUMPI: --blocks-per-rank must be 1, 2, 4 or 8\n");
         return GPUMPI_EINVAL;
     }
+    const bool one = o.one_cluster != 0;
+    if (one && (C != 1 || n > 16)) {
+        set_last_error("--one-cluster takes at most 16 ranks of one block each");
+        fprintf(stderr, "GPUMPI: --one-cluster takes at most 16 ranks of one block each\n");
+        return GPUMPI_EINVAL;
+    }
     int max_res = 0;
     int T = choose_threads(kernel, n * C, o.threads_per_rank, rank_smem_bytes(0), &max_res);
     if (T == 0 || T % 32 || T < 64 || T > 1024) {
@@ -560,8 +570,17 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         return GPUMPI_ENORES;
     }
     o.threads_per_rank = T;
-    const size_t smem = pick_rank_smem(kernel, T, n * C);
-    if (C > 1) {
+    size_t smem = pick_rank_smem(kernel, T, n * C);
+    if (one) {
+        // each block's mailbox at the end of its dynamic shared memory
+        smem += MB_SMEM_BYTES;
+        if (!allow_dynamic_smem(kernel, smem)) {
+            set_last_error("no room for the shared-memory mailboxes");
+            return GPUMPI_ENORES;
+        }
+        if (n > 8) HCHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    }
+    if (C > 1 || one) {
         // every cluster (rank) must be resident at once
         cudaLaunchConfig_t q;
         memset(&q, 0, sizeof(q));
@@ -570,14 +589,14 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         q.dynamicSmemBytes = smem;
         cudaLaunchAttribute qa[1];
         qa[0].id = cudaLaunchAttributeClusterDimension;
-        qa[0].val.clusterDim.x = C;
+        qa[0].val.clusterDim.x = one ? n : C;
         qa[0].val.clusterDim.y = 1;
         qa[0].val.clusterDim.z = 1;
         q.attrs = qa;
         q.numAttrs = 1;
         int clusters = 0;
         HCHECK(cudaOccupancyMaxActiveClusters(&clusters, kernel, &q));
-        if (clusters < n) {
+        if (clusters < (one ? 1 : n)) {
             char m[200];
             snprintf(m, sizeof(m), "%d ranks of %d blocks cannot all be resident (at most %d clusters fit)", n, C,
                      clusters);
@@ -635,12 +654,13 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
     L.slot_job = dslots;
     L.slot_rank = dslots + n;
     L.slot_base = 0;
+    L.job_cluster = one ? 1 : 0;
     void* args[] = {&L};
     if (o.verbose)
         fprintf(stderr, "GPUMPI: %d ranks x %d block(s) x %d threads, job memory %.1f MiB, heap %.1f MiB\n", n, C,
                 T, total / 1048576.0, o.heap_bytes / 1048576.0);
     const double t0 = now_s();
-    if (C == 1) {
+    if (C == 1 && !one) {
         HCHECK(cudaLaunchCooperativeKernel(kernel, dim3(n), dim3(T), args, smem, st));
     } else {
         cudaLaunchConfig_t cfg;
@@ -653,7 +673,7 @@ extern "C" int gpumpi_run_program(const void* kernel, int prog_argc, char** prog
         at[0].id = cudaLaunchAttributeCooperative;
         at[0].val.cooperative = 1;
         at[1].id = cudaLaunchAttributeClusterDimension;
-        at[1].val.clusterDim.x = C;
+        at[1].val.clusterDim.x = one ? n : C;
         at[1].val.clusterDim.y = 1;
         at[1].val.clusterDim.z = 1;
         cfg.attrs = at;

@@ -305,12 +305,61 @@ static __device__ __noinline__ void fold_push_t(const char* const* ptab, const c
     }
 }
 
+// Gather path for short folds (few elements, many inputs): the block first
+// loads all nin * m input elements into shared memory, 8 independent loads in
+// flight per thread, then thread i folds element i in rank order from there.
+// A thread-per-element fold would instead wait one memory round trip per
+// input (256 of them for a 256-rank communicator).  `g` is the gather area
+// (nin * m elements of T, shared memory).
+template <class T, class O>
+static __device__ void fold_gather(T* out, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi, int tid,
+                                   int T_, const char* const* ptab, T* g) {
+    const u64 m = hi - lo;
+    const u64 total = m * (u64)nin;
+    constexpr int U = 8;
+    for (u64 k0 = (u64)tid; k0 < total; k0 += (u64)U * T_) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const u64 k = k0 + (u64)u * T_;
+            if (k < total) v[u] = ldcg(in_ptr<T>(pub, (int)(k / m), in_off, ptab) + lo + k % m);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const u64 k = k0 + (u64)u * T_;
+            if (k < total) g[k] = v[u];
+        }
+    }
+    bsync();
+    for (u64 i = tid; i < m; i += T_) {
+        T acc = g[i];
+        for (int q = 1; q < nin; q++) acc = O::f(g[(u64)q * m + i], acc);
+        out[i] = acc;
+    }
+}
+
+// Shared memory available to fold_gather after the pointer table (bytes), and its start.
+static __device__ __forceinline__ u32 gather_bytes(int nin, char** at) {
+    extern __shared__ __align__(16) char gm_dsmem[];
+    const u32 tab = ((u32)nin * (u32)sizeof(char*) + 15u) & ~15u;
+    const u32 avail = bulk_stage_bytes();
+    *at = gm_dsmem + BCTX_BYTES + BULK_BAR_BYTES + tab;
+    return avail > tab ? avail - tab : 0;
+}
+
 // One out-of-line function per (type, operator): each gets its own register
 // allocation instead of sharing one across the whole dispatch switch.
 template <class T, class O>
 static __device__ __noinline__ void fold_t(void* outv, const Pub* pub, int nin, u64 in_off, u64 lo, u64 hi,
                                            int tid, int T_, const char* const* ptab) {
     T* out = reinterpret_cast<T*>(outv);
+    if (nin >= 8 && hi - lo <= 4 * (u64)T_) {
+        char* at = nullptr;
+        if ((hi - lo) * (u64)nin * sizeof(T) <= gather_bytes(nin, &at) && alignof(T) <= 16) {
+            fold_gather<T, O>(out, pub, nin, in_off, lo, hi, tid, T_, ptab, reinterpret_cast<T*>(at));
+            return;
+        }
+    }
     if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
         bool aligned = ((uintptr_t)out & 15) == 0;
         for (int q = 0; q < nin && aligned; q++)

@@ -35,8 +35,8 @@ static __device__ __forceinline__ char* eager_slot(Job* j, int world_rank, int s
 // Thread 0: claim a free slot in the destination's mailbox and fill its header.
 // Returns the slot, or -1 when the mailbox is full.
 static __device__ int claim_and_fill(Job* j, MPI_Request_impl* r) {
-    Mailbox* mb = &j->mbox[r->peer_world];
-    u64 used = ld_relaxed(&mb->used);
+    Mailbox* mb = mbox_of(r->peer_world);
+    u64 used = mb_ld(&mb->used);
     int s;
     for (;;) {
         u64 freeb = ~used;
@@ -45,11 +45,11 @@ static __device__ int claim_and_fill(Job* j, MPI_Request_impl* r) {
         u64 bit = 1ull << s;
         // acquire: a slot freed by the receiver's release of `used` is claimed
         // only after the receiver's clear of its ready bit
-        u64 old = atom_or_acquire(&mb->used, bit);
+        u64 old = mb_atom_or_acquire(&mb->used, bit);
         if (!(old & bit)) break;
         used = old | bit;
     }
-    u64 stamp = atomicAdd(&mb->stamp, 1ull);
+    u64 stamp = mb_atom_add(&mb->stamp, 1ull);
     MsgHdr& h = mb->hdr[s];
     const bool eager = r->bytes <= j->eager_bytes;
     h.ctx = r->ctx;
@@ -60,6 +60,16 @@ static __device__ int claim_and_fill(Job* j, MPI_Request_impl* r) {
     h.stamp = stamp;
     h.rdv_src = eager ? nullptr : r->buf;
     h.rdv_done = eager ? nullptr : (u32*)&r->done;
+    if (eager && r->bytes <= INLINE_BYTES && r->bytes) {
+        // the payload travels in the header
+        unsigned char tmp[INLINE_BYTES];
+        for (u64 i = 0; i < r->bytes; i++) tmp[i] = ((const unsigned char*)r->buf)[i];
+        for (u64 i = r->bytes; i < INLINE_BYTES; i++) tmp[i] = 0;
+        u64 w[2];
+        memcpy(w, tmp, INLINE_BYTES);
+        h.inl[0] = w[0];
+        h.inl[1] = w[1];
+    }
     return s;
 }
 
@@ -71,7 +81,7 @@ static __device__ void stage_delivery(MPI_Request_impl* r, int slot) {
     b.x.slot = slot;
     b.x.src = r->buf;
     b.x.dst = slot >= 0 ? eager_slot(j, r->peer_world, slot) : nullptr;
-    b.x.bytes = (slot >= 0 && eager) ? r->bytes : 0;
+    b.x.bytes = (slot >= 0 && eager && r->bytes > INLINE_BYTES) ? r->bytes : 0;
     b.x.peer = r->peer_world;
     b.x.a = eager;
 }
@@ -89,7 +99,7 @@ static __device__ void deliver_staged(MPI_Request_impl* r, int tid, int T) {
         r->state = eager ? RS_DONE : RS_WAIT_RDV;
         // release: the header and the payload copied by the block (ordered by
         // the barrier above) become visible before the ready bit
-        red_or_release(&b.job->mbox[peer].ready, 1ull << slot);
+        mb_red_or_release(&mbox_of(peer)->ready, 1ull << slot);
     }
 }
 
@@ -126,17 +136,18 @@ static __device__ int warp_match(u64 ready, int tid) {
     int best = -1;
     if (tid < 32) {
         const int ctx = b.x.ctx, src = b.x.peer, tag = b.x.tag;
-        Mailbox* mb = &b.job->mbox[b.rank];
+        Mailbox* mb = mbox_of(b.rank);
         u64 best_stamp = ~0ull;
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             const int s = tid + 32 * k;
             if ((ready >> s) & 1ull) {
                 const MsgHdr* h = &mb->hdr[s];
-                const int hctx = __ldcg(&h->ctx), hsrc = __ldcg(&h->src), htag = __ldcg(&h->tag);
+                const int4 h0 = mb_ld4(h);   // ctx, src, tag, kind
+                const int hctx = h0.x, hsrc = h0.y, htag = h0.z;
                 if (hctx == ctx && (src == MPI_ANY_SOURCE || hsrc == src) &&
                     (tag == MPI_ANY_TAG || htag == tag)) {
-                    const u64 st = __ldcg(&h->stamp);
+                    const u64 st = mb_ld(&h->stamp);
                     if (st < best_stamp) {
                         best_stamp = st;
                         best = s;
@@ -164,13 +175,13 @@ static __device__ int warp_match(u64 ready, int tid) {
 static __device__ int progress_recvs(int tid, int T) {
     BlockCtx& b = bctx();
     RankPriv* p = b.priv;
-    Mailbox* mb = &b.job->mbox[b.rank];
+    Mailbox* mb = mbox_of(b.rank);
     int did = 0;
     // thread-0 walk state
     int cur = -1, prev = -1;
     u64 ready = 0;
     if (tid == 0) {
-        ready = ld_acquire(&mb->ready);
+        ready = mb_ld_acquire(&mb->ready);
         cur = ready ? p->recv_head : -1;
     }
     for (;;) {
@@ -194,11 +205,21 @@ static __device__ int progress_recvs(int tid, int T) {
             if (best >= 0) {
                 const MPI_Request_impl* r = &p->reqs[cur];
                 const MsgHdr* h = &mb->hdr[best];
-                const u64 bytes = __ldcg(&h->bytes);
-                const int kind = __ldcg(&h->kind);
-                b.x.src = kind == 0 ? (const void*)eager_slot(b.job, b.rank, best) : ldcg(&h->rdv_src);
+                const u64 bytes = mb_ld(&h->bytes);
+                const int kind = mb_ld_int(&h->kind);
+                const u64 n = bytes < r->bytes ? bytes : r->bytes;
                 b.x.dst = r->buf;
-                b.x.bytes = bytes < r->bytes ? bytes : r->bytes;
+                if (kind == 0 && bytes <= INLINE_BYTES) {
+                    // the payload is in the header: the leader copies it
+                    const ulonglong2 w = mb_ld2(&h->inl);
+                    const unsigned char* pc = (const unsigned char*)&w;
+                    for (u64 i = 0; i < n; i++) ((unsigned char*)r->buf)[i] = pc[i];
+                    b.x.src = nullptr;
+                    b.x.bytes = 0;
+                } else {
+                    b.x.src = kind == 0 ? (const void*)eager_slot(b.job, b.rank, best) : (const void*)mb_ld((const u64*)&h->rdv_src);
+                    b.x.bytes = n;
+                }
             }
         }
         bsync();
@@ -209,21 +230,21 @@ static __device__ int progress_recvs(int tid, int T) {
             if (tid == 0) {
                 MPI_Request_impl* r = &p->reqs[cur];
                 const MsgHdr* h = &mb->hdr[slot];
-                const u64 bytes = __ldcg(&h->bytes);
-                const int kind = __ldcg(&h->kind);
-                r->st_source = __ldcg(&h->src);
-                r->st_tag = __ldcg(&h->tag);
+                const u64 bytes = mb_ld(&h->bytes);
+                const int4 h0 = mb_ld4(h);   // ctx, src, tag, kind
+                r->st_source = h0.y;
+                r->st_tag = h0.z;
                 r->st_bytes = bytes < r->bytes ? bytes : r->bytes;
                 r->st_err = bytes > r->bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
-                u32* done = kind == 1 ? ldcg(&h->rdv_done) : nullptr;
-                red_and_relaxed(&mb->ready, ~(1ull << slot));
+                u32* done = h0.w == 1 ? (u32*)mb_ld((const u64*)&h->rdv_done) : nullptr;
+                mb_red_and_relaxed(&mb->ready, ~(1ull << slot));
                 if (done) {
                     __threadfence();
                     st_release32(done, 1u);
                 }
                 // release: the ready clear and the reads of the slot come before
                 // the slot can be claimed again
-                red_and_release(&mb->used, ~(1ull << slot));
+                mb_red_and_release(&mb->used, ~(1ull << slot));
                 r->state = RS_DONE;
                 const int nxt = r->next;
                 if (prev >= 0) p->reqs[prev].next = nxt;
@@ -349,7 +370,7 @@ __device__ int p2p_wait(MPI_Request_impl* r, int tid, int T, int blocking) {
 __device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status* st, int tid,
                          int T) {
     BlockCtx& b = bctx();
-    Mailbox* mb = &b.job->mbox[b.rank];
+    Mailbox* mb = mbox_of(b.rank);
     u64 t0 = 0;
     unsigned ns = 32;
     if (tid == 0) t0 = gtime();
@@ -357,7 +378,7 @@ __device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status*
         int did = progress_deferred(tid, T);
         bsync();
         if (tid == 0) {
-            b.bval = ld_acquire(&mb->ready);
+            b.bval = mb_ld_acquire(&mb->ready);
             b.x.ctx = ctx;
             b.x.peer = source;
             b.x.tag = tag;
@@ -368,9 +389,10 @@ __device__ int p2p_probe(int source, int tag, int ctx, int blocking, MPI_Status*
         if (tid == 0 && best >= 0) {
             const MsgHdr* h = &mb->hdr[best];
             if (st) {
-                const u64 hb = __ldcg(&h->bytes);
-                st->MPI_SOURCE = __ldcg(&h->src);
-                st->MPI_TAG = __ldcg(&h->tag);
+                const u64 hb = mb_ld(&h->bytes);
+                const int4 h0 = mb_ld4(h);
+                st->MPI_SOURCE = h0.y;
+                st->MPI_TAG = h0.z;
                 st->MPI_ERROR = MPI_SUCCESS;
                 st->gpumpi_count_lo = (int)(hb & 0xffffffffu);
                 st->gpumpi_count_hi = (int)(hb >> 32);
@@ -447,7 +469,9 @@ __device__ bool p2p_send_fast(MPI_Request_impl* r) {
     const int slot = claim_and_fill(j, r);
     if (slot < 0) return false;
     char* dst = eager_slot(j, r->peer_world, slot);
-    if (bulk) {
+    if (r->bytes <= INLINE_BYTES) {
+        // claim_and_fill put the payload into the header
+    } else if (bulk) {
         const u64 n16 = r->bytes & ~(u64)15;
         const int rc = leader_bulk_copy(dst, (const char*)r->buf, n16);
         if (rc) {   // the job has failed; nothing is published
@@ -459,7 +483,7 @@ __device__ bool p2p_send_fast(MPI_Request_impl* r) {
     } else if (r->bytes) {
         leader_copy(dst, r->buf, r->bytes);
     }
-    red_or_release(&j->mbox[r->peer_world].ready, 1ull << slot);
+    mb_red_or_release(&mbox_of(r->peer_world)->ready, 1ull << slot);
     r->state = RS_DONE;
     return true;
 }
@@ -474,7 +498,7 @@ __device__ bool p2p_send_rdv_fast(MPI_Request_impl* r) {
     r->done = 0;
     const int slot = claim_and_fill(j, r);   // rendezvous header: rdv_src = r->buf, rdv_done = &r->done
     if (slot < 0) return false;
-    red_or_release(&j->mbox[r->peer_world].ready, 1ull << slot);
+    mb_red_or_release(&mbox_of(r->peer_world)->ready, 1ull << slot);
     r->state = RS_WAIT_RDV;
     return true;
 }
@@ -529,13 +553,13 @@ static __device__ int claim_slot_small(Mailbox* mb) {
     for (int tries = 0;; tries++) {
         if (~used == 0) {
             if (tries) return -1;
-            used = ld_relaxed(&mb->used);
+            used = mb_ld(&mb->used);
             if (~used == 0) return -1;
         }
         const int s = __ffsll((long long)~used) - 1;
         const u64 bit = 1ull << s;
         // acquire: the slot is written only after the receiver released it
-        const u64 old = atom_or_acquire(&mb->used, bit);
+        const u64 old = mb_atom_or_acquire(&mb->used, bit);
         if (!(old & bit)) {
             b.slot_hint = old | bit;
             return s;
@@ -552,8 +576,8 @@ static __device__ int claim_slot_small(Mailbox* mb) {
 __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc) {
     BlockCtx& b = bctx();
     if (!is_global(buf)) return 0;
-    Mailbox* mb = &b.mbox[dest_job];
-    const u64 stamp = atomicAdd(&mb->stamp, 1ull);
+    Mailbox* mb = mbox_of(dest_job);
+    const u64 stamp = mb_atom_add(&mb->stamp, 1ull);
     u32* done = &b.priv->rdv_done_small;
     *done = 0u;
     const int s = claim_slot_small(mb);
@@ -562,7 +586,7 @@ __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int 
     *(int4*)h = make_int4(ctx, me, tag, 1);   // kind = rendezvous
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
     *(ulonglong2*)&h->rdv_src = make_ulonglong2((u64)buf, (u64)done);
-    red_or_release(&mb->ready, 1ull << s);
+    mb_red_or_release(&mb->ready, 1ull << s);
     Job* j = b.job;
     const u64 t0 = gtime();
     unsigned ns = 32;
@@ -591,8 +615,8 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx,
     BlockCtx& b = bctx();
     const bool bulk = leader_bulk_ok(buf, bytes);
     if (bytes > FAST_MSG_BYTES && !bulk) return 0;
-    Mailbox* mb = &b.mbox[dest_job];
-    const u64 stamp = atomicAdd(&mb->stamp, 1ull);   // a skipped stamp only leaves a gap
+    Mailbox* mb = mbox_of(dest_job);
+    const u64 stamp = mb_atom_add(&mb->stamp, 1ull);   // a skipped stamp only leaves a gap
     // up to 64 aligned bytes are loaded now, while the atomics are in flight
     const bool pre = bytes <= 64 && ((uintptr_t)buf & 15) == 0;
     uint4 v[4];
@@ -608,7 +632,16 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx,
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
     char* slot = b.eager + ((u64)dest_job * MB_SLOTS + s) * b.eager_bytes;
     *rc = MPI_SUCCESS;
-    if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
+    if (bytes <= INLINE_BYTES) {   // the payload travels in the header
+        unsigned char tmp[INLINE_BYTES];
+        if (pre) {
+            memcpy(tmp, &v[0], INLINE_BYTES);
+        } else {
+            for (u64 i = 0; i < bytes; i++) tmp[i] = ((const unsigned char*)buf)[i];
+            for (u64 i = bytes; i < INLINE_BYTES; i++) tmp[i] = 0;
+        }
+        *(uint4*)&h->inl = *(const uint4*)tmp;
+    } else if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
 #pragma unroll
         for (int k = 0; k < 4; k++)
             if ((u64)k * 16 < bytes) ((uint4*)slot)[k] = v[k];
@@ -620,7 +653,7 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx,
     } else if (bytes) {
         leader_copy(slot, buf, bytes);
     }
-    red_or_release(&mb->ready, 1ull << s);
+    mb_red_or_release(&mb->ready, 1ull << s);
     return 1;
 }
 
@@ -629,7 +662,7 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx,
 struct SmallMatch {
     int slot, src, tag, kind;
     u64 bytes;
-    uint4 pre;   // the first 16 payload bytes of an eager message
+    uint4 pre;   // the payload of an eager message of at most INLINE_BYTES
 };
 
 // The oldest message among the `ready` slots matching (ctx, source, tag).  The
@@ -643,9 +676,9 @@ static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, in
     while (ready) {
         const int s = __ffsll((long long)ready) - 1;
         ready &= ready - 1;
-        const int4 h0 = __ldcg((const int4*)&mb->hdr[s]);
-        const ulonglong2 h1 = __ldcg((const ulonglong2*)&mb->hdr[s].bytes);
-        const uint4 p0 = __ldcg((const uint4*)(slots + (u64)s * b.eager_bytes));
+        const int4 h0 = mb_ld4(&mb->hdr[s]);
+        const ulonglong2 h1 = mb_ld2(&mb->hdr[s].bytes);
+        const ulonglong2 p0 = mb_ld2(&mb->hdr[s].inl);   // the payload when bytes <= INLINE_BYTES
         if (h0.x != ctx) continue;
         if (source != MPI_ANY_SOURCE && h0.y != source) continue;
         if (tag != MPI_ANY_TAG && h0.z != tag) continue;
@@ -656,7 +689,7 @@ static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, in
             m->tag = h0.z;
             m->kind = h0.w;
             m->bytes = h1.x;
-            m->pre = p0;
+            m->pre = *(const uint4*)&p0;
         }
     }
     return m->slot >= 0;
@@ -674,7 +707,7 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
     const char* rdv_src = nullptr;
     if (m.kind != 0) {
         // rendezvous: the leader pulls from the sender's buffer when the bulk engine applies
-        const ulonglong2 h2 = __ldcg((const ulonglong2*)&mb->hdr[m.slot].rdv_src);
+        const ulonglong2 h2 = mb_ld2(&mb->hdr[m.slot].rdv_src);
         rdv_src = (const char*)h2.x;
         rdv_done = (u32*)h2.y;
         if (!bulk || ((uintptr_t)rdv_src & 15) != 0) return 0;
@@ -689,7 +722,7 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
         *rc = leader_bulk_copy(d, src, n16);
         if (*rc) return 1;   // the job has failed; the slot stays claimed
         for (u64 i = n16; i < n; i++) d[i] = __ldcg(src + i);
-    } else if (n <= 16) {
+    } else if (m.bytes <= INLINE_BYTES) {
         const char* pc = (const char*)&m.pre;
         for (u64 i = 0; i < n; i++) d[i] = pc[i];
     } else {
@@ -703,12 +736,12 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
         }
         for (; i < n; i++) d[i] = __ldcg(src + i);
     }
-    red_and_relaxed(&mb->ready, ~(1ull << m.slot));
+    mb_red_and_relaxed(&mb->ready, ~(1ull << m.slot));
     if (rdv_done) {
         __threadfence();
         st_release32(rdv_done, 1u);
     }
-    red_and_release(&mb->used, ~(1ull << m.slot));
+    mb_red_and_release(&mb->used, ~(1ull << m.slot));
     *rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
     *got = n;
     return 1;
@@ -718,13 +751,13 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
 __device__ int p2p_recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st, int* rc) {
     BlockCtx& b = bctx();
     Job* j = b.job;
-    Mailbox* mb = &b.mbox[b.rank];
+    Mailbox* mb = mbox_of(b.rank);
     const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
     const u64 t0 = gtime();
     unsigned ns = 32;
     for (;;) {
         // acquire on every poll: nothing read after it comes from L1 anyway
-        const u64 ready = ld_acquire(&mb->ready);
+        const u64 ready = mb_ld_acquire(&mb->ready);
         SmallMatch m;
         if (ready && small_match(mb, slots, ready, ctx, source, tag, &m)) {
             u64 got = 0;
@@ -799,9 +832,9 @@ __device__ int lazy_materialize() {
 __device__ int lazy_progress() {
     BlockCtx& b = bctx();
     if (b.lazy_n == 0) return MPI_SUCCESS;
-    Mailbox* mb = &b.mbox[b.rank];
+    Mailbox* mb = mbox_of(b.rank);
     const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
-    u64 ready = ld_acquire(&mb->ready);
+    u64 ready = mb_ld_acquire(&mb->ready);
     RankPriv* p = b.priv;
     int i = 0;
     while (i < b.lazy_n && ready) {
@@ -860,21 +893,22 @@ __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled) {
     *handled = 0;
     // lazy receives were posted earlier and match first: the block path posts them, then r
     if (p->recv_head >= 0 || p->defer_head >= 0 || b.lazy_n) return MPI_SUCCESS;
-    Mailbox* mb = &j->mbox[b.rank];
+    Mailbox* mb = mbox_of(b.rank);
     const u64 t0 = gtime();
     unsigned ns = 32;
     for (;;) {
-        u64 ready = ld_acquire(&mb->ready);
+        u64 ready = mb_ld_acquire(&mb->ready);
         int best = -1;
         u64 best_stamp = ~0ull;
         while (ready) {
             const int s = __ffsll((long long)ready) - 1;
             ready &= ready - 1;
             const MsgHdr* h = &mb->hdr[s];
-            if (__ldcg(&h->ctx) != r->ctx) continue;
-            if (r->peer != MPI_ANY_SOURCE && __ldcg(&h->src) != r->peer) continue;
-            if (r->tag != MPI_ANY_TAG && __ldcg(&h->tag) != r->tag) continue;
-            const u64 st = __ldcg(&h->stamp);
+            const int4 h0 = mb_ld4(h);   // ctx, src, tag, kind
+            if (h0.x != r->ctx) continue;
+            if (r->peer != MPI_ANY_SOURCE && h0.y != r->peer) continue;
+            if (r->tag != MPI_ANY_TAG && h0.z != r->tag) continue;
+            const u64 st = mb_ld(&h->stamp);
             if (st < best_stamp) {
                 best_stamp = st;
                 best = s;
@@ -882,11 +916,16 @@ __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled) {
         }
         if (best >= 0) {
             const MsgHdr* h = &mb->hdr[best];
-            const u64 bytes = __ldcg(&h->bytes);
-            if (__ldcg(&h->kind) != 0 || bytes > FAST_MSG_BYTES) return MPI_SUCCESS;   // block path
+            const u64 bytes = mb_ld(&h->bytes);
+            const int4 h0 = mb_ld4(h);
+            if (h0.w != 0 || bytes > FAST_MSG_BYTES) return MPI_SUCCESS;   // block path
             const u64 n = bytes < r->bytes ? bytes : r->bytes;
             const char* src = eager_slot(j, b.rank, best);
-            if (n) {   // the slot is 16-byte aligned; the destination may not be
+            if (bytes <= INLINE_BYTES) {   // the payload is in the header
+                const ulonglong2 w = mb_ld2(&h->inl);
+                const char* pc = (const char*)&w;
+                for (u64 i = 0; i < n; i++) ((char*)r->buf)[i] = pc[i];
+            } else if (n) {   // the slot is 16-byte aligned; the destination may not be
                 char* d = (char*)r->buf;
                 u64 i = 0;
                 if (((uintptr_t)d & 15) == 0)
@@ -895,12 +934,12 @@ __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled) {
                     for (; i + 8 <= n; i += 8) *(u64*)(d + i) = __ldcg((const u64*)(src + i));
                 for (; i < n; i++) d[i] = __ldcg(src + i);
             }
-            r->st_source = __ldcg(&h->src);
-            r->st_tag = __ldcg(&h->tag);
+            r->st_source = h0.y;
+            r->st_tag = h0.z;
             r->st_bytes = n;
             r->st_err = bytes > r->bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
-            red_and_relaxed(&mb->ready, ~(1ull << best));
-            red_and_release(&mb->used, ~(1ull << best));
+            mb_red_and_relaxed(&mb->ready, ~(1ull << best));
+            mb_red_and_release(&mb->used, ~(1ull << best));
             r->state = RS_DONE;
             *handled = 1;
             return MPI_SUCCESS;

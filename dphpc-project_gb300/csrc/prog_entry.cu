@@ -14,6 +14,7 @@ extern __device__ int __gpu_max_threads();
 
 namespace gm {
 __device__ bool program_block_begin(const Launch& L);
+__device__ void program_block_end(const Launch& L);
 }
 
 // The name converted programs use for the start of dynamic shared memory
@@ -49,12 +50,16 @@ static __device__ void run_rank() {
 
 extern "C" __global__ void __launch_bounds__(1024) gpumpi_program_kernel(gm::Launch L) {
     using namespace gm;
-    if (!program_block_begin(L)) return;
+    if (!program_block_begin(L)) {
+        program_block_end(L);
+        return;
+    }
     if (bctx().cl_rank > 0) {   // a helper block of a cluster rank: shares of its parallel loops
         cluster_helper_loop();
         return;
     }
     run_rank();
+    program_block_end(L);
 }
 
 // Serving runtime (server.cu): blocks 0..nworkers-1 are rank slots that run

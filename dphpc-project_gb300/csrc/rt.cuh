@@ -77,13 +77,17 @@ struct MsgHdr {
     u64 stamp;          // arrival order at this receiver
     const void* rdv_src;
     u32* rdv_done;      // sender's completion word for rendezvous
-    u64 pad[2];
+    u64 inl[2];         // the payload of an eager message of at most INLINE_BYTES
 };
 static_assert(sizeof(MsgHdr) == 64, "MsgHdr layout");
+constexpr u64 INLINE_BYTES = 16;   // eager payloads up to this size travel in the header
 
 // Per-receiver mailbox.  Senders claim a slot by setting its bit in `used`,
 // fill the header (and the eager payload), then set the bit in `ready` with
-// release semantics.  Only the receiver clears bits.
+// release semantics.  Only the receiver clears bits.  A job whose ranks all
+// share one thread-block cluster keeps each rank's mailbox in its block's
+// shared memory (distributed shared memory for the senders); every access
+// therefore uses generic addresses (the mb_* primitives below).
 struct alignas(128) Mailbox {
     u64 used;
     u64 pad0[15];
@@ -364,6 +368,8 @@ struct Launch {
     int* slot_job;                // [nslots], -1 = idle
     int* slot_rank;               // [nslots]
     int slot_base;                // rank slot of block 0 (launches that run at once use disjoint ranges)
+    int job_cluster;              // 1: the launch is one cluster, one block per rank, mailboxes in
+                                  // shared memory (the job's rank r is the cluster's block r)
 };
 
 
@@ -443,6 +449,57 @@ __device__ __forceinline__ u64 ld_relaxed(const u64* p) {
     return v;
 }
 __device__ __forceinline__ bool is_global(const void* p) { return __isGlobal(p) != 0; }
+
+// Mailbox words and headers, by generic address: global memory, or the
+// shared memory of a block of this cluster.  Loads are L2-coherent (relaxed,
+// gpu scope) like ld.global.cg on global memory.
+__device__ __forceinline__ u64 mb_ld(const u64* p) {
+    u64 v;
+    asm volatile("ld.relaxed.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int mb_ld_int(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ u64 mb_ld_acquire(const u64* p) {
+    u64 v;
+    asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int4 mb_ld4(const void* p) {
+    int4 v;
+    asm volatile("ld.relaxed.gpu.v4.s32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ ulonglong2 mb_ld2(const void* p) {
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.v2.u64 {%0,%1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ u64 mb_atom_or_acquire(u64* p, u64 v) {
+    u64 old;
+    asm volatile("atom.acquire.gpu.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ u64 mb_atom_add(u64* p, u64 v) {
+    u64 old;
+    asm volatile("atom.relaxed.gpu.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void mb_red_or_release(u64* p, u64 v) {
+    asm volatile("red.release.gpu.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void mb_red_and_relaxed(u64* p, u64 v) {
+    asm volatile("red.relaxed.gpu.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void mb_red_and_release(u64* p, u64 v) {
+    asm volatile("red.release.gpu.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 
 // Loads of data written by other rank blocks go through L2 (ld.global.cg), so
 // a line this SM cached for an earlier message in the same slot or table entry
@@ -572,6 +629,8 @@ struct BlockCtx {
     // on the helper's cl_go barrier; helpers report completion through the
     // job's cl_done counter of the rank in global memory, so that no helper
     // ever touches the leader block's shared memory.
+    int mb_cluster;               // 1: mailboxes in the shared memory of the job's one cluster
+    Mailbox* mb_local;            // this block's shared-memory mailbox (generic address)
     int cl_n;
     int cl_rank;
     int cl_released;              // leader: the helpers were told to exit
@@ -585,6 +644,19 @@ struct BlockCtx {
 };
 
 static_assert(offsetof(BlockCtx, slot) == 0, "converted programs read the rank slot at offset 0");
+
+// The mailbox of job rank r (global memory, or block r of the job's cluster).
+__device__ __forceinline__ Mailbox* mbox_of(int r) {
+    extern __shared__ __align__(16) char gm_dsmem[];
+    const BlockCtx& b = *reinterpret_cast<const BlockCtx*>(gm_dsmem);
+    if (!b.mb_cluster) return b.mbox + r;
+    Mailbox* m;
+    asm("mapa.u64 %0, %1, %2;" : "=l"(m) : "l"(b.mb_local), "r"(r));
+    return m;
+}
+// Shared memory a block sets aside at the end of its dynamic shared memory for
+// its mailbox when the job is one cluster.
+constexpr int MB_SMEM_BYTES = (int)((sizeof(Mailbox) + 127) / 128 * 128);
 
 // Dynamic shared memory of a rank block: BlockCtx, then (when the launch
 // gave more) the bulk-copy area: mbarriers, then staging buffers.

@@ -154,7 +154,8 @@ static __device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cv
 __device__ u32 bulk_stage_bytes() {
     u32 dyn;
     asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
-    const u32 base = BCTX_BYTES + BULK_BAR_BYTES;
+    // a one-cluster job keeps its mailbox at the end of dynamic shared memory
+    const u32 base = BCTX_BYTES + BULK_BAR_BYTES + (bctx().mb_cluster ? (u32)MB_SMEM_BYTES : 0u);
     return dyn > base ? dyn - base : 0;
 }
 
@@ -484,6 +485,8 @@ static __device__ void block_ctx_init(Job* job, int rank, int slot, u32 C, u32 c
     b.cl_released = 0;
     b.cl_phase = 0;
     b.cl_cmd.op = -1;
+    b.mb_cluster = 0;
+    b.mb_local = nullptr;
     if (crank > 0) b.leader_mode = 0;   // a helper block of a cluster rank
 }
 
@@ -498,10 +501,15 @@ __device__ void rank_block_setup(Job* job, int rank, int slot) {
 // initialise the rank.  Returns false for idle slots.
 __device__ bool program_block_begin(const Launch& L) {
     BlockCtx& b = bctx();
-    // a rank is one cluster: C consecutive blocks (C = 1 without a cluster launch)
+    // a rank is one cluster: C consecutive blocks (C = 1 without a cluster
+    // launch, and for a job that is one cluster of one-block ranks)
     u32 C, crank;
     asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(C));
     asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(crank));
+    if (L.job_cluster) {
+        C = 1;
+        crank = 0;
+    }
     const int slot = (int)(blockIdx.x / C);
     if (threadIdx.x == 0) {
         const int jid = slot < L.nslots ? L.slot_job[slot] : -1;
@@ -509,13 +517,33 @@ __device__ bool program_block_begin(const Launch& L) {
             b.job = nullptr;
         } else {
             block_ctx_init(&L.jobs[jid], L.slot_rank[slot], L.slot_base + slot, C, crank);
+            if (L.job_cluster) {
+                extern __shared__ __align__(16) char gm_dsmem[];
+                u32 dyn;
+                asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+                b.mb_cluster = 1;
+                b.mb_local = reinterpret_cast<Mailbox*>(gm_dsmem + ((dyn - (u32)MB_SMEM_BYTES) & ~127u));
+            }
         }
     }
     __syncthreads();
+    if (L.job_cluster) {
+        // every block clears its mailbox before any block may write to it
+        if (b.job) blk_memset(b.mb_local, 0, sizeof(Mailbox), (int)threadIdx.x, (int)blockDim.x);
+        asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+    }
     if (!b.job) return false;
     if (crank == 0) rank_init((int)threadIdx.x, (int)blockDim.x);
     cluster_setup((int)threadIdx.x);
     return true;
+}
+
+// End of a block of a one-cluster job: its shared memory holds its rank's
+// mailbox, which the other ranks' blocks may address until every block is
+// done, so no block leaves before all have arrived here (threads that left
+// the kernel early, such as a leader that called exit(), do not count).
+__device__ void program_block_end(const Launch& L) {
+    if (L.job_cluster) asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
 
 

@@ -8,7 +8,8 @@
 // to fifteen other communicators, so the batched choice is measured in the
 // batched launch itself: for each co-resident thread count, every descriptor
 // takes its best schedule at that count, the whole list is timed, and at the
-// winning count each (collective, type) group tries every schedule in turn.
+// winning count each (collective, type) group tries every schedule in turn,
+// then flag rounds for its calls (`sync`) in a launch-ordered plan.
 // Timing: two untimed launches, then `reps` launches between CUDA events on
 // a stream of its own.  Plain results are cached, one line per shape, thread
 // count and GPU:
@@ -163,9 +164,10 @@ extern "C" int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_
     // ---- batched form, measured in the batched launch
     if (!rc && batched_threads) {
         std::vector<gpumpi_coll_desc> work(descs, descs + ndesc);
+        for (auto& d : work) d.sync = 0;
         double best_us = -1.0;
         int best_t = -1;
-        std::vector<int> best_algo(ndesc);
+        std::vector<int> best_algo(ndesc), best_sync(ndesc, 0);
         auto time_batched = [&](int t, double* us) -> int {
             gpumpi_plan_t plan = nullptr;
             const int prc = gpumpi_plan_create(work.data(), ndesc, t, 1, &plan);
@@ -201,28 +203,51 @@ extern "C" int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_
             if (std::find(groups.begin(), groups.end(), g) == groups.end()) groups.push_back(g);
         }
         for (size_t gi = 0; gi < groups.size() && !rc; gi++) {
+            auto in_group = [&](int i) {
+                return descs[i].op == groups[gi].first && descs[i].dtype == groups[gi].second;
+            };
             const std::vector<int> cands = algos_of(groups[gi].first);
-            if (cands.size() < 2) continue;
-            for (int algo : cands) {
-                for (int i = 0; i < ndesc; i++)
-                    work[i].algo = (descs[i].op == groups[gi].first && descs[i].dtype == groups[gi].second)
-                                       ? algo
-                                       : best_algo[i];
+            for (size_t ci = 0; cands.size() >= 2 && ci < cands.size() && !rc; ci++) {
+                for (int i = 0; i < ndesc; i++) {
+                    work[i].algo = in_group(i) ? cands[ci] : best_algo[i];
+                    work[i].sync = best_sync[i];
+                }
                 double us = 0.0;
                 rc = time_batched(kThreads[best_t], &us);
                 if (rc) break;
                 if (verbose)
                     fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d algo %d: %.2f us\n", groups[gi].first,
-                            groups[gi].second, algo, us);
+                            groups[gi].second, cands[ci], us);
                 if (us < best_us) {
                     best_us = us;
                     for (int i = 0; i < ndesc; i++) best_algo[i] = work[i].algo;
                 }
             }
+            if (rc) break;
+            // the group's calls with flag rounds (a launch-ordered plan leaves its
+            // ranks unsynchronised; readers of one buffer that run in step share
+            // its lines in L2)
+            for (int i = 0; i < ndesc; i++) {
+                work[i].algo = best_algo[i];
+                work[i].sync = in_group(i) ? 1 : best_sync[i];
+            }
+            double us = 0.0;
+            rc = time_batched(kThreads[best_t], &us);
+            if (rc) break;
+            if (verbose)
+                fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d with flag rounds: %.2f us\n",
+                        groups[gi].first, groups[gi].second, us);
+            if (us < best_us) {
+                best_us = us;
+                for (int i = 0; i < ndesc; i++) best_sync[i] = work[i].sync;
+            }
         }
         if (!rc) {
             *batched_threads = kThreads[best_t];
-            for (int i = 0; i < ndesc; i++) descs[i].algo = best_algo[i];
+            for (int i = 0; i < ndesc; i++) {
+                descs[i].algo = best_algo[i];
+                descs[i].sync = best_sync[i];
+            }
         }
     } else if (!rc) {
         for (int i = 0; i < ndesc; i++) descs[i].algo = plain_algos ? plain_algos[i] : descs[i].algo;

@@ -24,7 +24,7 @@ class Desc(ctypes.Structure):
         ("sendbufs", POINTER(c_void_p)),
         ("recvbufs", POINTER(c_void_p)),
         ("algo", c_int),
-        ("pad", c_int),
+        ("sync", c_int),
     ]
 
 
@@ -89,9 +89,9 @@ class TuneOpts(ctypes.Structure):
 
 
 def autotune(lib, descs: list, reps: int = 5, cache_path: str | None = None, verbose: bool = False):
-    """gpumpi_autotune: sets every descriptor's algo (the batched choice) in
-    place; returns (threads per rank of the batched launch, per-descriptor
-    plain-form threads, per-descriptor plain-form algos)."""
+    """gpumpi_autotune: sets every descriptor's algo and sync (the batched
+    choice) in place; returns (threads per rank of the batched launch,
+    per-descriptor plain-form threads, per-descriptor plain-form algos)."""
     arr = (Desc * len(descs))(*descs)
     plain = (c_int * len(descs))()
     palgo = (c_int * len(descs))()
@@ -101,6 +101,7 @@ def autotune(lib, descs: list, reps: int = 5, cache_path: str | None = None, ver
           "gpumpi_autotune")
     for i, d in enumerate(descs):
         d.algo = arr[i].algo
+        d.sync = arr[i].sync
     return bt.value, list(plain), list(palgo)
 
 

@@ -55,6 +55,8 @@ typedef struct gpumpi_opts {
     int verbose;             /* print GPUMPI: launch lines on stderr */
     int blocks_per_rank;     /* --blocks-per-rank: each rank a cluster of this many thread
                                 blocks (1, 2, 4, 8; 0 = 1); parallel loops span all of them */
+    int one_cluster;         /* --one-cluster: all ranks (at most 16) in one thread-block
+                                cluster, mailboxes in distributed shared memory */
 } gpumpi_opts;
 
 /* Exported by every program library: parse "---gpumpi" options from argv,
@@ -184,7 +186,7 @@ typedef struct gpumpi_comm_s* gpumpi_comm_t;
  *   ALLTOALL, ALLGATHER  1 peer blocks one after another by the whole rank
  *              block, 2 one peer block per warp, 3 all peer blocks through
  *              one bulk asynchronous copy pipeline (cp.async.bulk)
- * gpumpi_autotune fills it in. */
+ * gpumpi_autotune fills it in, and `sync` in the batched form. */
 typedef struct gpumpi_coll_desc {
     gpumpi_comm_t comm;
     int op;
@@ -195,7 +197,8 @@ typedef struct gpumpi_coll_desc {
     void* const* sendbufs;
     void* const* recvbufs;
     int algo;
-    int pad;
+    int sync;    /* 1: this call synchronises its ranks with flag rounds even in a
+                    launch-ordered plan (gpumpi_plan_set_sync); 0: the plan's form */
 } gpumpi_coll_desc;
 
 /* Create a communicator of nranks rank blocks with its synchronisation state in HBM. */

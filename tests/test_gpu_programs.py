@@ -190,3 +190,63 @@ def test_gpu_apps_with_cluster_ranks_match_oracle(gpu_built, prog, args, ranks, 
     key = "pic " if prog == "pic" else "is "
     strip = lambda lines: [ln for ln in lines if "-time" not in ln]
     assert strip(g.lines(key)) == strip(c.lines(key))
+
+
+# ---------------------------------------------------------------- one-cluster jobs (mailboxes in shared memory)
+
+ONE_CLUSTER_KAT = [c for c in KAT_CASES if c[0] in ("kat_p2p", "kat_coll") and c[2] <= 16]
+
+
+@pytest.mark.parametrize("prog,scenario,nranks", ONE_CLUSTER_KAT)
+def test_gpu_known_answers_in_one_cluster(gpu_built, prog, scenario, nranks):
+    """Every known-answer scenario of at most 16 ranks with the whole job in
+    one thread-block cluster: each rank's mailbox lives in its block's shared
+    memory and senders write headers and small payloads through distributed
+    shared memory."""
+    args = [scenario] if scenario else []
+    res = gpu_built.run_program(prog, args, nranks=nranks, extra=GPU_OPTS + ["--one-cluster"], timeout=180)
+    check_all_ok(res, scenario, nranks)
+
+
+@pytest.mark.parametrize("pattern,mode,lo,hi,iters,ranks,comm", [
+    ("pairs", "block", 3, 16, 10, 2, "world"),
+    ("pairs", "nb", 3, 20, 5, 8, "world"),
+    ("ring", "block", 3, 14, 10, 7, "dup"),
+    ("ring", "nb", 3, 12, 4, 16, "world"),
+])
+def test_gpu_p2p_sweep_in_one_cluster_matches_oracle(gpu_built, pattern, mode, lo, hi, iters, ranks, comm):
+    """The point-to-point sweep with the job in one cluster: every payload
+    intact and every checksum equal to the host MPI run's."""
+    args = [pattern, mode, str(lo), str(hi), str(iters), comm]
+    g = gpu_built.run_program("p2p_sweep", args, nranks=ranks, extra=GPU_OPTS + ["--one-cluster"], timeout=300)
+    c = run_oracle("p2p_sweep", args, nranks=ranks, timeout=300)
+    assert g.returncode == 0, g.stdout[-2000:] + g.stderr[-2000:]
+    got = g.lines("p2p ")
+    assert len(got) == hi - lo + 1 and all(" errors 0 " in ln for ln in got)
+    assert got == c.lines("p2p ")
+
+
+def test_gpu_pi_in_one_cluster_bit_exact(gpu_built):
+    g = gpu_built.run_program("pi", ["10000000"], nranks=8, extra=GPU_OPTS + ["--one-cluster"], timeout=180)
+    c = run_oracle("pi", ["10000000"], nranks=8, timeout=180)
+    assert g.returncode == 0, g.stderr
+    assert g.lines("pi bits") == c.lines("pi bits")
+
+
+def test_gpu_one_cluster_rejects_too_many_ranks(gpu_built):
+    res = gpu_built.run_program("pi", ["1000"], nranks=17, extra=GPU_OPTS + ["--one-cluster"], timeout=60)
+    assert res.returncode != 0
+    assert "one-cluster" in res.stderr
+
+
+@pytest.mark.parametrize("runs,blocks", [(64, 1), (4096, 1), (4096, 4)])
+def test_gpu_pi_parallel_runs_bit_exact(gpu_built, runs, blocks):
+    """pi with each rank's intervals summed as `runs` consecutive runs in a
+    parallel loop and the run sums added in order: the GPU (one or several
+    blocks per rank) and the host MPI build print the same bits."""
+    args = ["10000000", str(runs)]
+    g = gpu_built.run_program("pi", args, nranks=8, extra=GPU_OPTS + ["--blocks-per-rank", str(blocks)], timeout=180)
+    c = run_oracle("pi", args, nranks=8, timeout=180)
+    assert g.returncode == 0, g.stderr
+    assert g.lines("pi bits") == c.lines("pi bits")
+    assert g.lines("pi is approximately") == c.lines("pi is approximately")

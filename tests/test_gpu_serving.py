@@ -99,8 +99,7 @@ def test_online_submissions_run_beside_a_running_job(gpu_built):
     time.sleep(1.5)
     p.stdin.write(f"32 0 {' '.join(PIC_ARGS)}\n64 0 {' '.join(PIC_ARGS)}\n")
     p.stdin.flush()
-    p.stdin.close()
-    out, err = p.communicate(timeout=400)
+    out, err = p.communicate(timeout=400)   # closes standard input: no more jobs
     assert p.returncode == 0, out[-3000:] + err[-3000:]
     per_job = {k: [] for k in range(3)}
     times = {}
