@@ -410,6 +410,24 @@ def app_runs(host, timeout: float = 600.0) -> dict:
     return out
 
 
+def allocator_runs(host, lib) -> dict:
+    """Device malloc: the churn of the point-to-point configuration (every
+    thread, log-uniform 16 B - 4 KiB, up to 8 live objects) and the reference
+    allocator benchmark's shape (12 x 1024 threads, one 400-byte object each:
+    100 floats), on the runtime's slab allocator and on CUDA's device heap
+    (the reference's allocator)."""
+    out = {}
+    st = host.malloc_churn(lib, 1216, 256, 64, live=8, seed=3, heap_bytes=8 << 30)
+    out["churn_1216x256_threads"] = {k: st[k] for k in ("allocs", "failed", "corrupt", "ops_per_s",
+                                                         "malloc_cycles_p50", "malloc_cycles_p99",
+                                                         "malloc_cycles_mean", "free_cycles_mean")}
+    for name, cuda in (("reference_shape_12x1024_400B_slab", False), ("reference_shape_12x1024_400B_cuda_heap", True)):
+        st = host.malloc_bench(lib, 12, 1024, 400, heap_bytes=1 << 30, cuda_heap=cuda)
+        out[name] = {k: st[k] for k in ("allocs", "failed", "corrupt", "malloc_cycles_mean", "malloc_cycles_p50",
+                                        "malloc_cycles_p99", "free_cycles_mean", "free_cycles_p99", "seconds")}
+    return out
+
+
 def run_oracle_bench(lg: int, iters: int, ranks: int = 1024, timeout: float = 900):
     exe = os.path.join(ROOT, "oracle", "build", "bin", "coll_bench")
     if not os.path.exists(exe):
@@ -656,6 +674,14 @@ def main():
         h2d, d2h = e2e_step()
     esecs = time.perf_counter() - t0
     e2e_gbs = ebytes * e_steps / esecs / 1e9
+    # the same plans without the copies: the device share of an end-to-end step
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        for eplan, _, _, st, _ in eparts:
+            eplan.launch(st.cuda_stream)
+        for _, _, _, st, _ in eparts:
+            st.synchronize()
+    ekern = (time.perf_counter() - t0) / e_steps
     for ep in eplans:
         ep.close()
     del eparts
@@ -688,8 +714,10 @@ def main():
                    "sample": f"failed: {e}"}
 
     apps = None
+    allocator = None
     if rank == 0 and not args.no_apps:
         apps = app_runs(host)
+        allocator = allocator_runs(host, lib)
 
     if rank == 0:
         line = {
@@ -730,10 +758,12 @@ def main():
                          "algorithmic_bytes": int(nbytes)},
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne,
+                    "seconds_per_step": round(esecs / e_steps, 5), "plans_only_seconds_per_step": round(ekern, 5),
                     "form": "gpumpi_plan_run_host, the 16 communicators as 4 batched plans on 4 streams"},
             "sustained": sustained,
             "sweep": sweep,
             "apps": apps,
+            "allocator": allocator,
             "verified": True,
             "verification": {"what": "every call of the timed plan after the timed region: Bcast and Alltoall "
                                      "outputs compared with their sources in full, Allreduce outputs of every "

@@ -35,9 +35,11 @@ struct ChurnArgs {
     int iters;
     int live;
     int cuda_heap;
+    unsigned fixed_bytes;        // 0: log-uniform sizes; else every object has this size
     unsigned long long seed;
-    unsigned int* hist;          // [HIST_BUCKETS]
-    unsigned long long* count;   // allocs, frees, failed, corrupt, misaligned
+    unsigned int* hist;          // [HIST_BUCKETS] malloc latency
+    unsigned int* fhist;         // [HIST_BUCKETS] free latency
+    unsigned long long* count;   // allocs, frees, failed, corrupt, misaligned, malloc cycles, free cycles
 };
 
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
@@ -73,9 +75,13 @@ __device__ bool check(const unsigned char* p, unsigned n, unsigned tag) {
 template <bool CUDA_HEAP>
 __global__ void __launch_bounds__(1024) gpumpi_churn_kernel(ChurnArgs a) {
     __shared__ unsigned int hist[HIST_BUCKETS];
-    __shared__ unsigned long long cnt[5];
-    for (int i = threadIdx.x; i < HIST_BUCKETS; i += blockDim.x) hist[i] = 0;
-    if (threadIdx.x < 5) cnt[threadIdx.x] = 0;
+    __shared__ unsigned int fhist[HIST_BUCKETS];
+    __shared__ unsigned long long cnt[7];
+    for (int i = threadIdx.x; i < HIST_BUCKETS; i += blockDim.x) {
+        hist[i] = 0;
+        fhist[i] = 0;
+    }
+    if (threadIdx.x < 7) cnt[threadIdx.x] = 0;
     __syncthreads();
     const unsigned long long tid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long rng = mix64(a.seed ^ (tid * 0x9e3779b97f4a7c15ull));
@@ -83,11 +89,15 @@ __global__ void __launch_bounds__(1024) gpumpi_churn_kernel(ChurnArgs a) {
     unsigned size[CHURN_MAX_LIVE] = {};
     unsigned tag[CHURN_MAX_LIVE] = {};
     int head = 0, n = 0;
-    unsigned long long allocs = 0, frees = 0, failed = 0, corrupt = 0, misaligned = 0;
+    unsigned long long allocs = 0, frees = 0, failed = 0, corrupt = 0, misaligned = 0, mcyc = 0, fcyc = 0;
     auto release = [&](int k) {
         if (!check(ring[k], size[k], tag[k])) corrupt++;
+        const long long t0 = clock64();
         if (CUDA_HEAP) free(ring[k]);
         else heap_free(a.heap, ring[k]);
+        const long long dt = clock64() - t0;
+        atomicAdd(&fhist[bucket_of((unsigned long long)(dt > 0 ? dt : 0))], 1u);
+        fcyc += (unsigned long long)(dt > 0 ? dt : 0);
         frees++;
     };
     for (int it = 0; it < a.iters; it++) {
@@ -101,10 +111,12 @@ __global__ void __launch_bounds__(1024) gpumpi_churn_kernel(ChurnArgs a) {
         const double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);   // [0, 1)
         unsigned bytes = (unsigned)exp2(4.0 + 8.0 * u);
         if (bytes > 4095) bytes = 4095;
+        if (a.fixed_bytes) bytes = a.fixed_bytes;
         const long long t0 = clock64();
         unsigned char* p = CUDA_HEAP ? (unsigned char*)malloc(bytes) : (unsigned char*)heap_alloc(a.heap, bytes);
         const long long dt = clock64() - t0;
         atomicAdd(&hist[bucket_of((unsigned long long)(dt > 0 ? dt : 0))], 1u);
+        mcyc += (unsigned long long)(dt > 0 ? dt : 0);
         allocs++;
         if (!p) {
             failed++;
@@ -128,10 +140,14 @@ __global__ void __launch_bounds__(1024) gpumpi_churn_kernel(ChurnArgs a) {
     atomicAdd(&cnt[2], failed);
     atomicAdd(&cnt[3], corrupt);
     atomicAdd(&cnt[4], misaligned);
+    atomicAdd(&cnt[5], mcyc);
+    atomicAdd(&cnt[6], fcyc);
     __syncthreads();
-    for (int i = threadIdx.x; i < HIST_BUCKETS; i += blockDim.x)
+    for (int i = threadIdx.x; i < HIST_BUCKETS; i += blockDim.x) {
         if (hist[i]) atomicAdd(&a.hist[i], hist[i]);
-    if (threadIdx.x < 5) atomicAdd(&a.count[threadIdx.x], cnt[threadIdx.x]);
+        if (fhist[i]) atomicAdd(&a.fhist[i], fhist[i]);
+    }
+    if (threadIdx.x < 7) atomicAdd(&a.count[threadIdx.x], cnt[threadIdx.x]);
 }
 
 // Lower edge of a histogram bucket, in cycles.
@@ -168,6 +184,9 @@ unsigned long long percentile(const unsigned long long* h, double q) {
 
 }  // namespace
 
+static int churn_run(int blocks, int threads, int iters, int live, uint64_t seed, size_t heap_bytes,
+                     int cuda_heap, unsigned fixed_bytes, void* stream, gpumpi_churn_stats* out);
+
 extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live, uint64_t seed,
                                    size_t heap_bytes, int cuda_heap, void* stream, gpumpi_churn_stats* out) {
     if (!out || blocks < 1 || threads < 32 || threads > 1024 || threads % 32 || iters < 0 || live < 1 ||
@@ -175,6 +194,20 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
         set_last_error("gpumpi_malloc_churn: bad arguments (live must be 1..16, threads 32..1024)");
         return GPUMPI_EINVAL;
     }
+    return churn_run(blocks, threads, iters, live, seed, heap_bytes, cuda_heap, 0, stream, out);
+}
+
+extern "C" int gpumpi_malloc_bench(int blocks, int threads, size_t bytes, size_t heap_bytes, int cuda_heap,
+                                   void* stream, gpumpi_churn_stats* out) {
+    if (!out || blocks < 1 || threads < 32 || threads > 1024 || threads % 32 || bytes < 1 || bytes > (1u << 20)) {
+        set_last_error("gpumpi_malloc_bench: bad arguments (threads 32..1024, bytes 1..1 MiB)");
+        return GPUMPI_EINVAL;
+    }
+    return churn_run(blocks, threads, 1, 1, 1, heap_bytes, cuda_heap, (unsigned)bytes, stream, out);
+}
+
+static int churn_run(int blocks, int threads, int iters, int live, uint64_t seed, size_t heap_bytes,
+                     int cuda_heap, unsigned fixed_bytes, void* stream, gpumpi_churn_stats* out) {
     if (heap_bytes == 0) heap_bytes = (size_t)4 << 30;
     memset(out, 0, sizeof(*out));
     int rc = GPUMPI_OK;
@@ -188,7 +221,8 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
     // metadata (64-bit bitmaps updated with 64-bit atomics) and the page lists.
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t o_hist = al(sizeof(Heap));
-    const size_t o_cnt = al(o_hist + HIST_BUCKETS * sizeof(unsigned));
+    const size_t o_fhist = al(o_hist + HIST_BUCKETS * sizeof(unsigned));
+    const size_t o_cnt = al(o_fhist + HIST_BUCKETS * sizeof(unsigned));
     const size_t o_ctl = al(o_cnt + 8 * sizeof(unsigned long long));
     const size_t o_meta = al(o_ctl + ctl);
     const size_t o_clsp = al(o_meta + meta);
@@ -196,8 +230,8 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
     char* mem = nullptr;
     char* heap_mem = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    unsigned hist32[HIST_BUCKETS];
-    unsigned long long hist[HIST_BUCKETS], cnt[5];
+    unsigned hist32[HIST_BUCKETS], fhist32[HIST_BUCKETS];
+    unsigned long long hist[HIST_BUCKETS], fhist[HIST_BUCKETS], cnt[7];
     float ms = 0;
     Heap h;
     ChurnArgs a;
@@ -228,7 +262,9 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
         a.live = live;
         a.cuda_heap = cuda_heap;
         a.seed = seed;
+        a.fixed_bytes = fixed_bytes;
         a.hist = dhist;
+        a.fhist = (unsigned*)(mem + o_fhist);
         a.count = dcnt;
     }
     if (cuda_heap) {
@@ -246,8 +282,12 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
     HK(cudaStreamSynchronize(st));
     HK(cudaEventElapsedTime(&ms, e0, e1));
     HK(cudaMemcpy(hist32, a.hist, sizeof(hist32), cudaMemcpyDeviceToHost));
+    HK(cudaMemcpy(fhist32, a.fhist, sizeof(fhist32), cudaMemcpyDeviceToHost));
     HK(cudaMemcpy(cnt, a.count, sizeof(cnt), cudaMemcpyDeviceToHost));
-    for (int i = 0; i < HIST_BUCKETS; i++) hist[i] = hist32[i];
+    for (int i = 0; i < HIST_BUCKETS; i++) {
+        hist[i] = hist32[i];
+        fhist[i] = fhist32[i];
+    }
     out->allocs = cnt[0];
     out->frees = cnt[1];
     out->failed = cnt[2];
@@ -257,6 +297,10 @@ extern "C" int gpumpi_malloc_churn(int blocks, int threads, int iters, int live,
     out->ops_per_s = ms > 0 ? (double)(cnt[0] + cnt[1]) / (ms / 1000.0) : 0.0;
     out->malloc_cycles_p50 = percentile(hist, 0.50);
     out->malloc_cycles_p99 = percentile(hist, 0.99);
+    out->malloc_cycles_mean = cnt[0] ? cnt[5] / cnt[0] : 0;
+    out->free_cycles_p50 = percentile(fhist, 0.50);
+    out->free_cycles_p99 = percentile(fhist, 0.99);
+    out->free_cycles_mean = cnt[1] ? cnt[6] / cnt[1] : 0;
     if (!cuda_heap) {
         unsigned st8[8];
         HK(cudaMemcpy(st8, h.stats, sizeof(st8), cudaMemcpyDeviceToHost));

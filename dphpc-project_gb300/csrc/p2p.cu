@@ -47,7 +47,7 @@ static __device__ int claim_and_fill(Job* j, MPI_Request_impl* r) {
         // only after the receiver's clear of its ready bit
         u64 old = mb_atom_or_acquire(&mb->used, bit);
         if (!(old & bit)) break;
-        used = old | bit;
+        used |= old | bit;   // old holds the bit's 32-bit half only
     }
     u64 stamp = mb_atom_add(&mb->stamp, 1ull);
     MsgHdr& h = mb->hdr[s];
@@ -559,12 +559,12 @@ static __device__ int claim_slot_small(Mailbox* mb) {
         const int s = __ffsll((long long)~used) - 1;
         const u64 bit = 1ull << s;
         // acquire: the slot is written only after the receiver released it
-        const u64 old = mb_atom_or_acquire(&mb->used, bit);
+        const u64 old = mb_atom_or_acquire(&mb->used, bit);   // the bit's 32-bit half
         if (!(old & bit)) {
-            b.slot_hint = old | bit;
+            b.slot_hint = (used & ((bit >> 32) ? 0xffffffffull : ~0xffffffffull)) | old | bit;
             return s;
         }
-        used = old | bit;
+        used |= old | bit;
     }
 }
 

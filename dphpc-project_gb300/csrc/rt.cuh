@@ -481,24 +481,40 @@ __device__ __forceinline__ ulonglong2 mb_ld2(const void* p) {
     asm volatile("ld.relaxed.gpu.v2.u64 {%0,%1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ u64 mb_atom_or_acquire(u64* p, u64 v) {
-    u64 old;
-    asm volatile("atom.acquire.gpu.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
-    return old;
+// The slot masks change one bit at a time, with 32-bit atomics on the half of
+// the 64-bit word that holds the bit: on distributed shared memory the 64-bit
+// bitwise atomics lost updates when several blocks hit one word (a bounded
+// probe on GB300 received 2.5-3.0 thousand of 14 thousand messages through the
+// 64-bit forms and all of them through the 32-bit forms).
+__device__ __forceinline__ u32* mb_half(u64* p, u64 bit) {
+    return reinterpret_cast<u32*>(p) + ((bit >> 32) ? 1 : 0);
 }
+__device__ __forceinline__ u32 mb_bit32(u64 bit) { return (bit >> 32) ? (u32)(bit >> 32) : (u32)bit; }
+// Set one bit; returns the old value of the bit's half in its place (the other half reads 0).
+__device__ __forceinline__ u64 mb_atom_or_acquire(u64* p, u64 bit) {
+    u32 old;
+    asm volatile("atom.acquire.gpu.or.b32 %0, [%1], %2;" : "=r"(old) : "l"(mb_half(p, bit)), "r"(mb_bit32(bit))
+                 : "memory");
+    return (bit >> 32) ? ((u64)old << 32) : (u64)old;
+}
+// Arrival counter (32 bits: stamps of one receiver's messages within a job).
 __device__ __forceinline__ u64 mb_atom_add(u64* p, u64 v) {
-    u64 old;
-    asm volatile("atom.relaxed.gpu.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
-    return old;
+    u32 old;
+    asm volatile("atom.relaxed.gpu.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(reinterpret_cast<u32*>(p)), "r"((u32)v)
+                 : "memory");
+    return (u64)old;
 }
-__device__ __forceinline__ void mb_red_or_release(u64* p, u64 v) {
-    asm volatile("red.release.gpu.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void mb_red_or_release(u64* p, u64 bit) {
+    asm volatile("red.release.gpu.or.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(mb_bit32(bit)) : "memory");
 }
-__device__ __forceinline__ void mb_red_and_relaxed(u64* p, u64 v) {
-    asm volatile("red.relaxed.gpu.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+// Clear one bit: mask = ~bit.
+__device__ __forceinline__ void mb_red_and_relaxed(u64* p, u64 mask) {
+    const u64 bit = ~mask;
+    asm volatile("red.relaxed.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
 }
-__device__ __forceinline__ void mb_red_and_release(u64* p, u64 v) {
-    asm volatile("red.release.gpu.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void mb_red_and_release(u64* p, u64 mask) {
+    const u64 bit = ~mask;
+    asm volatile("red.release.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
 }
 
 // Loads of data written by other rank blocks go through L2 (ld.global.cg), so

@@ -71,7 +71,9 @@ class ChurnStats(ctypes.Structure):
                 ("corrupt", ctypes.c_uint64), ("misaligned", ctypes.c_uint64), ("seconds", ctypes.c_double),
                 ("ops_per_s", ctypes.c_double), ("malloc_cycles_p50", ctypes.c_uint64),
                 ("malloc_cycles_p99", ctypes.c_uint64), ("fresh_pages", ctypes.c_uint64),
-                ("partial_pops", ctypes.c_uint64), ("partial_full", ctypes.c_uint64)]
+                ("partial_pops", ctypes.c_uint64), ("partial_full", ctypes.c_uint64),
+                ("malloc_cycles_mean", ctypes.c_uint64), ("free_cycles_p50", ctypes.c_uint64),
+                ("free_cycles_p99", ctypes.c_uint64), ("free_cycles_mean", ctypes.c_uint64)]
 
 
 def malloc_churn(lib: ctypes.CDLL, blocks: int, threads: int, iters: int, live: int = 8, seed: int = 1,
@@ -86,4 +88,20 @@ def malloc_churn(lib: ctypes.CDLL, blocks: int, threads: int, iters: int, live: 
     rc = f(blocks, threads, iters, live, seed, heap_bytes, int(cuda_heap), None, ctypes.byref(st))
     if rc != 0:
         raise RuntimeError(f"gpumpi_malloc_churn failed ({rc}): {lib.gpumpi_last_error().decode()}")
+    return {k: getattr(st, k) for k, _ in ChurnStats._fields_}
+
+
+def malloc_bench(lib: ctypes.CDLL, blocks: int = 12, threads: int = 1024, nbytes: int = 400,
+                 heap_bytes: int = 0, cuda_heap: bool = False) -> dict:
+    """gpumpi_malloc_bench: one malloc / write / check / free per thread (the
+    reference allocator benchmark's shape); returns its stats."""
+    f = lib.gpumpi_malloc_bench
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.POINTER(ChurnStats)]
+    f.restype = ctypes.c_int
+    lib.gpumpi_last_error.restype = ctypes.c_char_p
+    st = ChurnStats()
+    rc = f(blocks, threads, nbytes, heap_bytes, int(cuda_heap), None, ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"gpumpi_malloc_bench failed ({rc}): {lib.gpumpi_last_error().decode()}")
     return {k: getattr(st, k) for k, _ in ChurnStats._fields_}

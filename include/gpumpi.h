@@ -304,6 +304,10 @@ typedef struct gpumpi_churn_stats {
     uint64_t fresh_pages;         /* slab allocator: 64 KiB pages taken from the bump pointer */
     uint64_t partial_pops;        /*   pages taken from the free-chunk stacks */
     uint64_t partial_full;        /*   of those, pages that were full again */
+    uint64_t malloc_cycles_mean;  /* mean malloc latency (SM cycles, exact) */
+    uint64_t free_cycles_p50;     /* free latency percentiles (bucket lower edges) */
+    uint64_t free_cycles_p99;
+    uint64_t free_cycles_mean;    /* mean free latency */
 } gpumpi_churn_stats;
 
 /* Every thread of a blocks x threads grid runs `iters` rounds of: malloc of
@@ -315,6 +319,15 @@ typedef struct gpumpi_churn_stats {
  * Allocates and frees its own device memory; synchronises `stream`. */
 int gpumpi_malloc_churn(int blocks, int threads, int iters, int live, uint64_t seed, size_t heap_bytes,
                         int cuda_heap, void* stream, gpumpi_churn_stats* out);
+
+/* The reference's allocator benchmark shape (dynamic_allocator/
+ * benchmarks_template.cu:68-202): every thread of a blocks x threads grid
+ * allocates one object of `bytes` bytes, writes and checks it, and frees it;
+ * the latency of every malloc and free is recorded (mean and percentiles in
+ * `out`; allocs/frees/failed/corrupt as in gpumpi_malloc_churn).  cuda_heap
+ * as there.  Allocates and frees its own device memory; synchronises `stream`. */
+int gpumpi_malloc_bench(int blocks, int threads, size_t bytes, size_t heap_bytes, int cuda_heap, void* stream,
+                        gpumpi_churn_stats* out);
 
 /* Number of kernel launches this process issued through the collective API. */
 uint64_t gpumpi_kernel_launches(void);
