@@ -410,6 +410,32 @@ def app_runs(host, timeout: float = 600.0) -> dict:
     return out
 
 
+def serving_run(host, timeout: float = 600.0) -> dict:
+    """The PIC configuration served: 9 jobs of 16, 32 and 64 ranks (full
+    grid, 50 cycles) arriving every 200 ms on one server; makespan and the
+    50th/99th percentile of job latency (arrival to end) from the server's
+    own report, and each job's exit status."""
+    import tempfile
+    lines = [f"{n} {200 * k} 50 256 128 125 10\n" for k, n in enumerate([16, 32, 64] * 3)]
+    with tempfile.NamedTemporaryFile("w", suffix=".jobs", delete=False) as f:
+        f.writelines(lines)
+        path = f.name
+    try:
+        exe = os.path.join(host.BIN, "pic")
+        r = subprocess.run([exe, "---gpumpi", "--serve", path, "-t", "128", "-p", "2G", "--max-seconds", "300"],
+                           capture_output=True, text=True, timeout=timeout)
+    finally:
+        os.unlink(path)
+    m = re.search(r"serve summary jobs (\d+) makespan ([0-9.]+) latency_p50 ([0-9.]+) latency_p99 ([0-9.]+)",
+                  r.stdout)
+    exits = [int(x) for x in re.findall(r"serve job \d+ ranks \d+ exit (\d+)", r.stdout)]
+    if r.returncode or not m:
+        return {"error": (r.stdout[-300:] + r.stderr[-300:])}
+    return {"jobs": int(m.group(1)), "ranks": "16/32/64 x 3", "arrival_ms": 200, "makespan_s": float(m.group(2)),
+            "latency_p50_s": float(m.group(3)), "latency_p99_s": float(m.group(4)),
+            "all_exit_0": all(e == 0 for e in exits) and len(exits) == 9}
+
+
 def allocator_runs(host, lib) -> dict:
     """Device malloc: the churn of the point-to-point configuration (every
     thread, log-uniform 16 B - 4 KiB, up to 8 live objects) and the reference
@@ -717,6 +743,7 @@ def main():
     allocator = None
     if rank == 0 and not args.no_apps:
         apps = app_runs(host)
+        apps["serving_pic_9_jobs"] = serving_run(host)
         allocator = allocator_runs(host, lib)
 
     if rank == 0:

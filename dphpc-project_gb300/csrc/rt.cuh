@@ -450,72 +450,6 @@ __device__ __forceinline__ u64 ld_relaxed(const u64* p) {
 }
 __device__ __forceinline__ bool is_global(const void* p) { return __isGlobal(p) != 0; }
 
-// Mailbox words and headers, by generic address: global memory, or the
-// shared memory of a block of this cluster.  Loads are L2-coherent (relaxed,
-// gpu scope) like ld.global.cg on global memory.
-__device__ __forceinline__ u64 mb_ld(const u64* p) {
-    u64 v;
-    asm volatile("ld.relaxed.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ int mb_ld_int(const int* p) {
-    int v;
-    asm volatile("ld.relaxed.gpu.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ u64 mb_ld_acquire(const u64* p) {
-    u64 v;
-    asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ int4 mb_ld4(const void* p) {
-    int4 v;
-    asm volatile("ld.relaxed.gpu.v4.s32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p)
-                 : "memory");
-    return v;
-}
-__device__ __forceinline__ ulonglong2 mb_ld2(const void* p) {
-    ulonglong2 v;
-    asm volatile("ld.relaxed.gpu.v2.u64 {%0,%1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
-    return v;
-}
-// The slot masks change one bit at a time, with 32-bit atomics on the half of
-// the 64-bit word that holds the bit: on distributed shared memory the 64-bit
-// bitwise atomics lost updates when several blocks hit one word (a bounded
-// probe on GB300 received 2.5-3.0 thousand of 14 thousand messages through the
-// 64-bit forms and all of them through the 32-bit forms).
-__device__ __forceinline__ u32* mb_half(u64* p, u64 bit) {
-    return reinterpret_cast<u32*>(p) + ((bit >> 32) ? 1 : 0);
-}
-__device__ __forceinline__ u32 mb_bit32(u64 bit) { return (bit >> 32) ? (u32)(bit >> 32) : (u32)bit; }
-// Set one bit; returns the old value of the bit's half in its place (the other half reads 0).
-__device__ __forceinline__ u64 mb_atom_or_acquire(u64* p, u64 bit) {
-    u32 old;
-    asm volatile("atom.acquire.gpu.or.b32 %0, [%1], %2;" : "=r"(old) : "l"(mb_half(p, bit)), "r"(mb_bit32(bit))
-                 : "memory");
-    return (bit >> 32) ? ((u64)old << 32) : (u64)old;
-}
-// Arrival counter (32 bits: stamps of one receiver's messages within a job).
-__device__ __forceinline__ u64 mb_atom_add(u64* p, u64 v) {
-    u32 old;
-    asm volatile("atom.relaxed.gpu.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(reinterpret_cast<u32*>(p)), "r"((u32)v)
-                 : "memory");
-    return (u64)old;
-}
-__device__ __forceinline__ void mb_red_or_release(u64* p, u64 bit) {
-    asm volatile("red.release.gpu.or.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(mb_bit32(bit)) : "memory");
-}
-// Clear one bit: mask = ~bit.
-__device__ __forceinline__ void mb_red_and_relaxed(u64* p, u64 mask) {
-    const u64 bit = ~mask;
-    asm volatile("red.relaxed.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
-}
-__device__ __forceinline__ void mb_red_and_release(u64* p, u64 mask) {
-    const u64 bit = ~mask;
-    asm volatile("red.release.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
-}
 
 // Loads of data written by other rank blocks go through L2 (ld.global.cg), so
 // a line this SM cached for an earlier message in the same slot or table entry
@@ -688,6 +622,87 @@ __host__ __device__ constexpr size_t rank_smem_bytes(size_t stage) {
 __device__ __forceinline__ BlockCtx& bctx() {
     extern __shared__ __align__(16) char gm_dsmem[];
     return *reinterpret_cast<BlockCtx*>(gm_dsmem);
+}
+
+// Mailbox words and headers, by generic address: global memory, or the
+// shared memory of a block of this cluster.  Loads are L2-coherent (relaxed,
+// gpu scope) like ld.global.cg on global memory.
+__device__ __forceinline__ u64 mb_ld(const u64* p) {
+    u64 v;
+    asm volatile("ld.relaxed.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int mb_ld_int(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// Mailbox release/acquire: cluster scope when every rank of the job shares one
+// cluster (its mailboxes and all its senders are in the cluster), else gpu.
+__device__ __forceinline__ bool mb_in_cluster() { return bctx().mb_cluster != 0; }
+__device__ __forceinline__ u64 mb_ld_acquire(const u64* p) {
+    u64 v;
+    if (mb_in_cluster()) asm volatile("ld.acquire.cluster.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    else asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int4 mb_ld4(const void* p) {
+    int4 v;
+    asm volatile("ld.relaxed.gpu.v4.s32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ ulonglong2 mb_ld2(const void* p) {
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.v2.u64 {%0,%1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+    return v;
+}
+// The slot masks change one bit at a time, with 32-bit atomics on the half of
+// the 64-bit word that holds the bit: on distributed shared memory the 64-bit
+// bitwise atomics lost updates when several blocks hit one word (a bounded
+// probe on GB300 received 2.5-3.0 thousand of 14 thousand messages through the
+// 64-bit forms and all of them through the 32-bit forms).
+__device__ __forceinline__ u32* mb_half(u64* p, u64 bit) {
+    return reinterpret_cast<u32*>(p) + ((bit >> 32) ? 1 : 0);
+}
+__device__ __forceinline__ u32 mb_bit32(u64 bit) { return (bit >> 32) ? (u32)(bit >> 32) : (u32)bit; }
+// Set one bit; returns the old value of the bit's half in its place (the other half reads 0).
+__device__ __forceinline__ u64 mb_atom_or_acquire(u64* p, u64 bit) {
+    u32 old;
+    if (mb_in_cluster())
+        asm volatile("atom.acquire.cluster.or.b32 %0, [%1], %2;" : "=r"(old) : "l"(mb_half(p, bit)),
+                     "r"(mb_bit32(bit)) : "memory");
+    else
+        asm volatile("atom.acquire.gpu.or.b32 %0, [%1], %2;" : "=r"(old) : "l"(mb_half(p, bit)), "r"(mb_bit32(bit))
+                     : "memory");
+    return (bit >> 32) ? ((u64)old << 32) : (u64)old;
+}
+// Arrival counter (32 bits: stamps of one receiver's messages within a job).
+__device__ __forceinline__ u64 mb_atom_add(u64* p, u64 v) {
+    u32 old;
+    asm volatile("atom.relaxed.gpu.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(reinterpret_cast<u32*>(p)), "r"((u32)v)
+                 : "memory");
+    return (u64)old;
+}
+__device__ __forceinline__ void mb_red_or_release(u64* p, u64 bit) {
+    if (mb_in_cluster())
+        asm volatile("red.release.cluster.or.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(mb_bit32(bit)) : "memory");
+    else
+        asm volatile("red.release.gpu.or.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(mb_bit32(bit)) : "memory");
+}
+// Clear one bit: mask = ~bit.
+__device__ __forceinline__ void mb_red_and_relaxed(u64* p, u64 mask) {
+    const u64 bit = ~mask;
+    asm volatile("red.relaxed.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
+}
+__device__ __forceinline__ void mb_red_and_release(u64* p, u64 mask) {
+    const u64 bit = ~mask;
+    if (mb_in_cluster())
+        asm volatile("red.release.cluster.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
+    else
+        asm volatile("red.release.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
 }
 
 // Intra-call barrier of all threads of the rank block.

@@ -36,12 +36,13 @@ def _rank_fold(xs, op):
 
 
 @pytest.mark.parametrize("algo", [0, 1, 2, 3])
-@pytest.mark.parametrize("form", ["plain", "batched", "graph", "plain-flags", "graph-flags"])
+@pytest.mark.parametrize("form", ["plain", "batched", "graph", "plain-flags", "graph-flags", "graph-mixed"])
 @pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (32, 1 << 16)])
 def test_capi_collectives(coll, form, nranks, count, algo):
     """Every schedule (algo 1-3 and the size-based choice 0) folds in rank
     order, so each gives the host fold's bits, in the launch-ordered forms
-    (the calls are independent) and with flag rounds (-flags)."""
+    (the calls are independent), with flag rounds (-flags) and with both in
+    one launch (-mixed)."""
     import torch
 
     mod, lib = coll
@@ -80,6 +81,10 @@ def test_capi_collectives(coll, form, nranks, count, algo):
         # Reduce has schedules 1 and 2; Allreduce 1-3 (3: every rank pushes its
         # segment); Alltoall/Allgather 1-3 (3: bulk engine)
         d.algo = 2 if (d.op == mod.COLL_REDUCE and algo == 3) else algo
+    if form.endswith("-mixed"):
+        # every other call keeps its flag rounds inside the launch-ordered plan
+        for i, d in enumerate(descs):
+            d.sync = i % 2
     plan = mod.Plan(lib, descs, threads=128, batched=not form.startswith("plain"))
     assert plan.launch_ordered
     if form.endswith("-flags"):
