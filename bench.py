@@ -112,11 +112,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# DRAM bytes (read + write) of one batched launch, from ncu captures
-# (dram__bytes_read.sum + dram__bytes_write.sum, one pass): at the full 2^20
-# elements per rank, and at 2^15, which other per-rank counts scale from.
-NCU_TRAFFIC_BYTES_2_20 = 27657256704 + 39027092480
-NCU_TRAFFIC_BYTES_2_15 = 0.979630336e9 + 1.461430e9
+# DRAM bytes (read + write) of one batched launch at 2^16 elements per rank,
+# from a one-pass ncu capture of dram__bytes_read.sum + dram__bytes_write.sum
+# (profiles/gpumpi_plan_kernel_batched_collectives.md); other per-rank counts
+# scale it by their elements per rank.
+NCU_TRAFFIC_BYTES_2_16 = 1832801280 + 2687147776
 
 
 ALL_KINDS = ("bcast", "allreduce", "alltoall")
@@ -776,12 +776,10 @@ def main():
                       "batched_over_tuned_plain": round(value / world / plain_tuned_gbs, 2) if plain_tuned_gbs else None},
             "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind,
-                         "traffic": (NCU_TRAFFIC_BYTES_2_20 if n == 1 << 20 else
-                                     int(NCU_TRAFFIC_BYTES_2_15 * n / (1 << 15))) if kinds == ALL_KINDS else None,
-                         "traffic_note": ("bytes per launch, ncu DRAM read+write of this launch at 2^20 elements "
-                                          "per rank" if n == 1 << 20 else
-                                          "bytes per launch, ncu DRAM read+write at 2^15 elements per rank "
-                                          "scaled by elements per rank"),
+                         "traffic": int(NCU_TRAFFIC_BYTES_2_16 * n / (1 << 16)) if kinds == ALL_KINDS else None,
+                         "traffic_note": ("bytes per launch: ncu DRAM read+write of the same launch at 2^16 "
+                                          "elements per rank (4.52 GB, 1.12x its algorithmic bytes), scaled by "
+                                          "elements per rank"),
                          "algorithmic_bytes": int(nbytes)},
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne,

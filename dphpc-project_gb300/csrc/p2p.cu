@@ -716,6 +716,17 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
     }
     char* d = (char*)buf;
     *got = 0;
+    if (!bulk && m.kind == 0 && m.bytes <= INLINE_BYTES) {
+        // the payload is already in registers: free the slot first, so that
+        // the release waits for no store, then write the user's buffer
+        mb_red_and_relaxed(&mb->ready, ~(1ull << m.slot));
+        mb_red_and_release(&mb->used, ~(1ull << m.slot));
+        const char* pc = (const char*)&m.pre;
+        for (u64 i = 0; i < n; i++) d[i] = pc[i];
+        *rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
+        *got = n;
+        return 1;
+    }
     if (bulk) {
         const u64 n16 = n & ~(u64)15;
         const char* src = rdv_src ? rdv_src : slots + (u64)m.slot * b.eager_bytes;
