@@ -454,6 +454,26 @@ def allocator_runs(host, lib) -> dict:
     return out
 
 
+def host_link(torch, nbytes: int = 1 << 30, reps: int = 3) -> dict:
+    """Pinned host <-> device copy bandwidth of this machine right now (GB/s):
+    the ceiling of the end-to-end leg, whose copies dominate its time."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = round(nbytes * reps / (e0.elapsed_time(e1) / 1000.0) / 1e9, 1)
+    del h, d
+    return out
+
+
 def run_oracle_bench(lg: int, iters: int, ranks: int = 1024, timeout: float = 900):
     exe = os.path.join(ROOT, "oracle", "build", "bin", "coll_bench")
     if not os.path.exists(exe):
@@ -656,6 +676,7 @@ def main():
     # one plan's device-to-host copies then overlap the next plan's host-to-
     # device copies (the host link carries both directions at once).
     ne = 1 << args.e2e_lg
+    link = host_link(torch)
     ecomms, eplans, eparts = [], [], []
     for gi, group in enumerate(E2E_GROUPS):
         eplan, gcomms, gkeep, gitems, gdescs = build_plan(coll, lib, torch, group, ne, True, threads, seed=2 + gi)
@@ -784,6 +805,7 @@ def main():
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne,
                     "seconds_per_step": round(esecs / e_steps, 5), "plans_only_seconds_per_step": round(ekern, 5),
+                    "host_link_GBps": link,
                     "form": "gpumpi_plan_run_host, the 16 communicators as 4 batched plans on 4 streams"},
             "sustained": sustained,
             "sweep": sweep,

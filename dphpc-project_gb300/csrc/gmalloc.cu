@@ -13,9 +13,11 @@
 // empty does a claim take a fresh page.  Requests above 32 KiB take runs of
 // whole pages from one address-ordered list of free runs (first fit, split on
 // allocation, merged with both neighbours on free) or, when no run fits, from
-// the bump pointer.  The list sits behind a lock whose wait is bounded by the
-// global timer (a wait that runs out returns NULL); large requests are rare,
-// so the lock is not a hot spot.
+// the bump pointer (without the lock while no free run exists).  The list sits
+// behind a test-and-test-and-set lock whose wait is bounded by the global timer
+// (a wait that runs out returns NULL); a free walks the address-ordered list,
+// so thousands of large frees at once serialise on it (see the allocator
+// tests for the sizes covered).
 //
 // This replaces CUDA's device malloc (gpu_libs/gpu_libc/stdlib.cu:70-91) and
 // the reference's experimental coalescing allocators (gpu_libs/gpu_malloc/*),
@@ -240,19 +242,36 @@ static __device__ void* small_alloc(Heap* h, int c) {
     return result;
 }
 
+// Test-and-test-and-set with exponential back-off: waiters read the lock word
+// and try the CAS only when it looks free, so thousands of waiters do not
+// queue atomics in front of the holder's release.
 static __device__ bool large_lock(Heap* h) {
     if (atomicCAS(h->large_lock, 0u, 1u) != 0u) {
         const u64 t0 = gtime();
-        while (atomicCAS(h->large_lock, 0u, 1u) != 0u) {
+        unsigned ns = 64;
+        for (;;) {
+            if (*(volatile u32*)h->large_lock == 0u && atomicCAS(h->large_lock, 0u, 1u) == 0u) break;
             if (gtime() - t0 > LOCK_WAIT_NS) {
                 atomicAdd(&h->stats[2], 1u);
                 return false;
             }
-            __nanosleep(64);
+            __nanosleep(ns);
+            if (ns < 8192) ns <<= 1;
         }
     }
     __threadfence();
     return true;
+}
+
+// Fresh pages from the bump pointer need no lock (a failed request moves nothing).
+static __device__ u32 large_bump(Heap* h, u32 n) {
+    u32 first = *(volatile u32*)h->next_page;
+    while ((u64)first + n <= h->npages) {
+        const u32 seen = atomicCAS(h->next_page, first, first + n);
+        if (seen == first) return first;
+        first = seen;
+    }
+    return NO_PAGE;
 }
 
 static __device__ void large_unlock(Heap* h) {
@@ -264,6 +283,17 @@ static __device__ void* large_alloc(Heap* h, u64 bytes) {
     const u64 n64 = (bytes + PAGE - 1) / PAGE;
     if (n64 > h->npages) return nullptr;
     const u32 n = (u32)n64;
+    if (*(volatile u32*)h->large_head == 0) {
+        // no free run to reuse: take fresh pages without the lock (the pages
+        // of a fresh run belong to this caller alone, so are its page records)
+        const u32 p = large_bump(h, n);
+        if (p != NO_PAGE) {
+            h->meta[p].npages = n;
+            h->meta[p].cls = CLS_LARGE;
+            __threadfence();
+            return h->base + (u64)p * PAGE;
+        }
+    }
     if (!large_lock(h)) return nullptr;
     volatile PageMeta* meta = h->meta;
     u32 p = NO_PAGE;
@@ -290,17 +320,7 @@ static __device__ void* large_alloc(Heap* h, u64 bytes) {
         prev = c;
         cur = nxt;
     }
-    if (p == NO_PAGE) {   // bump pointer, only when the run fits (a failed request moves nothing)
-        u32 first = *(volatile u32*)h->next_page;
-        while ((u64)first + n <= h->npages) {
-            const u32 seen = atomicCAS(h->next_page, first, first + n);
-            if (seen == first) {
-                p = first;
-                break;
-            }
-            first = seen;
-        }
-    }
+    if (p == NO_PAGE) p = large_bump(h, n);   // only when the run fits
     if (p != NO_PAGE) {
         meta[p].cls = CLS_LARGE;
         meta[p].npages = n;

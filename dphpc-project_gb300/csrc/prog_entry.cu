@@ -73,16 +73,22 @@ extern "C" __global__ void __launch_bounds__(1024) gpumpi_server_kernel(gm::Serv
         return;
     }
     const int w = (int)blockIdx.x;
+    if (threadIdx.x == 0) {
+        u32 sm;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+        A.worker_sm[w] = (int)sm;
+        __threadfence();
+    }
     u64 seen = 0;
     Job* job;
-    int rank;
-    while (server_take(A, w, &seen, &job, &rank)) {
-        rank_block_setup(job, rank, A.slot_base + w);
+    int rank, slot;
+    while (server_take(A, w, &seen, &job, &rank, &slot)) {
+        rank_block_setup(job, rank, A.slot_base + slot);
         run_rank();
-        if (threadIdx.x != 0 && bctx().priv->exited) {
+        if (threadIdx.x != 0 && *(volatile int*)&bctx().priv->exited) {
             // the leader thread has left the kernel (exit(), abort(), a failed assert)
             if (threadIdx.x == 1) {
-                A.lost[w] = 1;
+                A.lost[slot] = 1;
                 __threadfence();
             }
             return;

@@ -329,7 +329,7 @@ constexpr int SERVE_RING = 256;       // records of each ring
 constexpr int SERVE_MAX_JOBS = 256;   // jobs running at once
 struct AdmitRec {
     Job* job;                         // the job's device record (in its memory, initialised)
-    int slot_base;                    // ranks r run on worker blocks slot_base + r
+    int slot_base;                    // rank r runs in rank slot slot_base + r
     int nranks;
     u64 ticket;
 };
@@ -354,7 +354,10 @@ struct ServerArgs {
     u64* assign_seq;                  // [nworkers] assignment counter; ~0 = stop
     Job** assign_job;                 // [nworkers]
     int* assign_rank;                 // [nworkers]
-    int* lost;                        // [nworkers] 1: the block left (a rank called exit())
+    int* assign_slot;                 // [nworkers] rank slot of the assigned rank
+    int* worker_sm;                   // [nworkers] SM each worker block runs on (written at start)
+    const int* perm;                  // [nworkers] rank slot -> worker block (slots interleave the SMs)
+    int* lost;                        // [nworkers] by rank slot: 1 = its block left (a rank called exit())
     ServeActive* active;              // [SERVE_MAX_JOBS] admin block's table
     int nworkers;
     int slot_base;                    // rank slot of worker block 0
@@ -853,7 +856,7 @@ __device__ void cluster_helper_loop();                        // helper blocks
 
 // serving runtime (csrc/server.cu)
 __device__ void server_admin(const ServerArgs& A);
-__device__ bool server_take(const ServerArgs& A, int w, u64* seen, Job** job, int* rank);
+__device__ bool server_take(const ServerArgs& A, int w, u64* seen, Job** job, int* rank, int* slot);
 __device__ void rank_block_setup(Job* job, int rank, int slot);   // every thread; one-block rank
 
 // rank lifecycle

@@ -143,7 +143,8 @@ struct gpumpi_server_s {
     char* ctl = nullptr;             // device: worker assignments, lost flags, admin table
     int* lost_d = nullptr;
     cudaStream_t kst = nullptr, cst = nullptr;
-    std::vector<char> slot_state;    // 0 idle, 1 running a job, 2 lost
+    std::vector<char> slot_state;    // by rank slot: 0 idle, 1 running a job, 2 lost
+    int nsm = 0;                     // SMs the worker blocks run on
     char* zeros = nullptr;           // pinned: sources of the job memory initialisation
     char* ones = nullptr;
     size_t fill_bytes = 0;
@@ -391,10 +392,12 @@ extern "C" int gpumpi_server_start(const void* kernel, const gpumpi_serve_opts* 
     memset(s->ones, 0xff, s->fill_bytes);
     const size_t W = (size_t)s->nworkers;
     const size_t o_seq = 0, o_job = o_seq + 8 * W, o_rank = o_job + 8 * W, o_lost = o_rank + 4 * W;
-    const size_t o_act = round_up(o_lost + 4 * W, 256);
+    const size_t o_slot = o_lost + 4 * W, o_sm = o_slot + 4 * W, o_perm = o_sm + 4 * W;
+    const size_t o_act = round_up(o_perm + 4 * W, 256);
     const size_t ctl_bytes = o_act + sizeof(ServeActive) * SERVE_MAX_JOBS;
     SCHECK(cudaMalloc(&s->ctl, ctl_bytes));
     SCHECK(cudaMemset(s->ctl, 0, ctl_bytes));
+    SCHECK(cudaMemset(s->ctl + o_sm, 0xff, 4 * W));   // -1 until each worker reports its SM
     s->lost_d = (int*)(s->ctl + o_lost);
     SCHECK(cudaStreamCreateWithFlags(&s->kst, cudaStreamNonBlocking));
     SCHECK(cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking));
@@ -406,12 +409,44 @@ extern "C" int gpumpi_server_start(const void* kernel, const gpumpi_serve_opts* 
     A.assign_seq = (u64*)(s->ctl + o_seq);
     A.assign_job = (Job**)(s->ctl + o_job);
     A.assign_rank = (int*)(s->ctl + o_rank);
+    A.assign_slot = (int*)(s->ctl + o_slot);
+    A.worker_sm = (int*)(s->ctl + o_sm);
+    A.perm = (const int*)(s->ctl + o_perm);
     A.lost = s->lost_d;
     A.active = (ServeActive*)(s->ctl + o_act);
     A.nworkers = s->nworkers;
     A.slot_base = 0;
     void* args[] = {&A};
     SCHECK(cudaLaunchCooperativeKernel(kernel, dim3(nblocks), dim3(T), args, smem, s->kst));
+    // Rank slots over worker blocks: every worker reports its SM, then slot k
+    // goes to the (k / nsm)-th worker of the (k mod nsm)-th SM, so that the
+    // consecutive slots of one job lie on different SMs.  Until the map is in
+    // device memory no job is admitted (the admin block reads it only then).
+    {
+        std::vector<int> sm(W, -1);
+        const double tw = now_seconds();
+        for (;;) {
+            SCHECK(cudaMemcpyAsync(sm.data(), s->ctl + o_sm, 4 * W, cudaMemcpyDeviceToHost, s->cst));
+            SCHECK(cudaStreamSynchronize(s->cst));
+            if (std::find(sm.begin(), sm.end(), -1) == sm.end()) break;
+            if (now_seconds() - tw > 30.0) {
+                set_last_error("gpumpi_server_start: worker blocks did not start");
+                __atomic_store_n(&s->ring_h->kill, 1, __ATOMIC_RELEASE);
+                cudaStreamSynchronize(s->kst);
+                return GPUMPI_ECUDA;
+            }
+            usleep(100);
+        }
+        std::map<int, std::vector<int>> by_sm;
+        for (size_t w = 0; w < W; w++) by_sm[sm[w]].push_back((int)w);
+        std::vector<int> perm;
+        for (size_t layer = 0; perm.size() < W; layer++)
+            for (auto& kv : by_sm)
+                if (layer < kv.second.size()) perm.push_back(kv.second[layer]);
+        SCHECK(cudaMemcpyAsync(s->ctl + o_perm, perm.data(), 4 * W, cudaMemcpyHostToDevice, s->cst));
+        SCHECK(cudaStreamSynchronize(s->cst));
+        s->nsm = (int)by_sm.size();
+    }
     s->t0 = now_seconds();
     if (so.verbose)
         fprintf(stderr, "GPUMPI serve: %d worker blocks of %d threads, pool %.1f MiB\n", s->nworkers, T,

@@ -9,8 +9,11 @@
 // polling of the admission ring and its completion records; workers wait on
 // device memory.  Every job keeps its own memory (mailboxes, tables, heap,
 // output) in the HBM pool for its whole life; a worker block runs one rank of
-// one job at a time, with the rank slot of the block, so the converted
-// globals of ranks that run at the same time never alias.
+// one job at a time, in the rank slot the admin block gives it, so the
+// converted globals of ranks that run at the same time never alias.  Rank
+// slots map to worker blocks so that consecutive slots sit on different SMs
+// (the host orders the blocks by the SM each reports at start): the ranks of
+// one job, which take consecutive slots, spread over the GPU.
 #include "rt.cuh"
 
 namespace gm {
@@ -86,9 +89,11 @@ __device__ void server_admin(const ServerArgs& A) {
                 __threadfence();
                 seq++;
                 for (int r = 0; r < s_rec.nranks; r++) {
-                    const int w = s_rec.slot_base + r;
+                    const int sl = s_rec.slot_base + r;
+                    const int w = A.perm[sl];
                     A.assign_job[w] = s_rec.job;
                     A.assign_rank[w] = r;
+                    A.assign_slot[w] = sl;
                     __threadfence();
                     st_release(&A.assign_seq[w], seq);
                 }
@@ -109,9 +114,9 @@ __device__ void server_admin(const ServerArgs& A) {
 
 // Worker block (every thread): wait for the next rank handed to block w (a
 // poll of device memory only).  False once the server ends.
-__device__ bool server_take(const ServerArgs& A, int w, u64* seen, Job** job, int* rank) {
+__device__ bool server_take(const ServerArgs& A, int w, u64* seen, Job** job, int* rank, int* slot) {
     __shared__ Job* s_job;
-    __shared__ int s_rank;
+    __shared__ int s_rank, s_slot;
     if (threadIdx.x == 0) {
         unsigned ns = 128;
         u64 v;
@@ -122,10 +127,12 @@ __device__ bool server_take(const ServerArgs& A, int w, u64* seen, Job** job, in
         *seen = v;
         s_job = v == ~0ull ? nullptr : A.assign_job[w];
         s_rank = A.assign_rank[w];
+        s_slot = A.assign_slot[w];
     }
     __syncthreads();
     *job = s_job;
     *rank = s_rank;
+    *slot = s_slot;
     __syncthreads();
     return *job != nullptr;
 }
