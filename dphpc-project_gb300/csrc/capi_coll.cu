@@ -73,6 +73,7 @@ static __device__ int run_desc(const DevDesc& d, MPI_Comm_impl* comm, int P, int
         a.rbuf = rb;
         switch (d.op) {
             case GPUMPI_COLL_BCAST:
+                if (d.algo == 2) break;   // the tree forwards copies made in this launch: flag rounds
                 a.count = d.count * d.esize;
                 return coll_lo_bcast(a, d.pub, P, rank, tid, T);
             case GPUMPI_COLL_REDUCE:
@@ -419,7 +420,7 @@ extern "C" int gpumpi_plan_create_ex(const gpumpi_coll_desc* descs, int ndesc, i
             return GPUMPI_EINVAL;
         if ((d.op == GPUMPI_COLL_BCAST || d.op == GPUMPI_COLL_REDUCE) && (d.root < 0 || d.root >= d.comm->n))
             return GPUMPI_EINVAL;
-        if (d.algo < 0 || d.algo > 3) return GPUMPI_EINVAL;
+        if (d.algo < 0 || d.algo > 4) return GPUMPI_EINVAL;
         auto it = std::find(comms.begin(), comms.end(), d.comm);
         cidx[i] = (int)(it - comms.begin());
         if (it == comms.end()) comms.push_back(d.comm);

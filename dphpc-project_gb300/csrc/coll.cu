@@ -177,6 +177,44 @@ __device__ int coll_barrier(MPI_Comm_impl* c, int tid, int T) {
 }
 
 // ---------------------------------------------------------------- bcast
+// Binomial tree (algo 2): with v = (rank - root) mod P, rank v copies from
+// v with its lowest set bit cleared once that rank has its copy (its
+// `arrive` flag), then raises its own; each rank returns once the ranks it
+// feeds (v + 2^k below its lowest set bit) have copied from it (their
+// `depart` flags).  log2(P) rounds, each reading a buffer at most log2(P)
+// ranks read, against one round in which P - 1 ranks read the root's buffer.
+static __device__ int bcast_tree(const CollArgs& a, u64 seq, int tid, int T) {
+    const BlockCtx::CommView* cs = &bctx().cv;
+    const int P = cs->P, me = cs->me, root = a.root;
+    const int v = (me - root + P) % P;
+    Pub p = {};
+    p.sbuf = a.rbuf;
+    if (v != 0) {
+        const int pv = v & (v - 1);
+        const int parent = (pv + root) % P;
+        int rc = wait_one(cs->arrive, parent, seq, tid);
+        if (rc) return rc;
+        blk_copy(a.rbuf, ldcg(&cs->pub[parent].sbuf), a.count, tid, T);
+        bsync();
+        if (tid == 0) cs->pub[me] = p;
+        raise_flag(cs->arrive, me, seq, tid);
+        raise_flag(cs->depart, me, seq, tid);
+    } else {
+        if (tid == 0) cs->pub[me] = p;
+        raise_flag(cs->arrive, me, seq, tid);
+    }
+    // the ranks this one feeds: v + 2^k for 2^k below v's lowest set bit (all k for the root)
+    const int low = v ? (v & -v) : (1 << 30);
+    int rc = MPI_SUCCESS;
+    if (tid == 0) {
+        for (int k = 1; k < low && v + k < P; k <<= 1) {
+            rc = wait_ge(&cs->depart[(v + k + root) % P], seq);
+            if (rc) break;
+        }
+    }
+    return (int)bcast(rc, tid);
+}
+
 // a.rbuf = buffer, a.count = bytes.
 __device__ int coll_bcast(const CollArgs& a, int tid, int T) {
     MPI_Comm_impl* c = a.comm;
@@ -184,6 +222,7 @@ __device__ int coll_bcast(const CollArgs& a, int tid, int T) {
     const u64 seq = coll_begin(c, tid);
     const int P = cs->P, me = cs->me, root = a.root;
     if (P == 1 || a.count == 0) return MPI_SUCCESS;
+    if (a.algo == 2) return bcast_tree(a, seq, tid, T);
     if (me == root) {
         Pub p = {};
         p.sbuf = a.rbuf;
@@ -585,19 +624,58 @@ __device__ int coll_lo_allreduce(const CollArgs& a, const Pub* pub, int P, int m
 // Alltoall / Allgather with a uniform block of a.count elements of a.rsize
 // bytes: block q of this rank's a.rbuf comes from rank q (Alltoall: its block
 // for this rank; Allgather: its whole send buffer).
+// Schedule 4 (and the choice for blocks of TINY_BLOCK_BYTES to BULK_SEG_MIN
+// when the buffers are 16-byte aligned): the 16-byte vectors of all P blocks
+// form one index space spread over every thread of the rank block, 8 loads in
+// flight per thread, the source bases in a shared-memory table.  Per-warp or
+// per-block copies of such blocks leave most threads idle (a 512-byte block
+// is one vector per lane of one warp) and wait one round trip per block.
+static __device__ bool alltoall_flat(const CollArgs& a, const Pub* pub, int P, int me, int gather, u64 b, int tid,
+                                     int T) {
+    extern __shared__ __align__(16) char gm_dsmem[];
+    if (b % 16 != 0 || bulk_stage_bytes() < (u32)P * sizeof(char*) || ((uintptr_t)a.rbuf & 15)) return false;
+    const char** tab = reinterpret_cast<const char**>(gm_dsmem + BCTX_BYTES + BULK_BAR_BYTES);
+    int bad = 0;
+    for (int q = tid; q < P; q += T) {
+        tab[q] = (const char*)ldcg(&pub[q].sbuf) + (gather ? 0 : (u64)me * b);
+        bad |= ((uintptr_t)tab[q] & 15) != 0;
+    }
+    if (bar_or(bad, T)) return false;   // the same answer on every rank: all see the same table
+    const u64 nv = b / 16, total = (u64)P * nv;
+    uint4* out = reinterpret_cast<uint4*>(a.rbuf);
+    constexpr int U = 8;
+    for (u64 k0 = (u64)tid; k0 < total; k0 += (u64)U * T) {
+        uint4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const u64 k = k0 + (u64)u * T;
+            if (k < total) v[u] = __ldcg(reinterpret_cast<const uint4*>(tab[k / nv]) + k % nv);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const u64 k = k0 + (u64)u * T;
+            if (k < total) out[k] = v[u];
+        }
+    }
+    bsync();
+    return true;
+}
+
 __device__ int coll_lo_alltoall(const CollArgs& a, const Pub* pub, int P, int me, int gather, int tid, int T) {
     const u64 b = a.count * (u64)a.rsize;
     if (b == 0) {
         bsync();
         return MPI_SUCCESS;
     }
+    const bool flat = a.algo == 4 || (a.algo == 0 && b > TINY_BLOCK_BYTES && b < BULK_SEG_MIN);
+    if (flat && alltoall_flat(a, pub, P, me, gather, b, tid, T)) return MPI_SUCCESS;
     auto blk = [&](int q, const void** s, void** d, u64* nb) -> bool {
         *s = (const char*)ldcg(&pub[q].sbuf) + (gather ? 0 : (u64)me * b);
         *d = (char*)a.rbuf + (u64)q * b;
         *nb = b;
         return true;
     };
-    multi_copy(P, me, b, blk, tid, T, a.algo);
+    multi_copy(P, me, b, blk, tid, T, a.algo == 4 ? 0 : a.algo);
     return MPI_SUCCESS;
 }
 

@@ -29,7 +29,9 @@ namespace gm {
 
 constexpr u32 PAGE = 64 * 1024;
 constexpr int NCLS = 12;
-constexpr int HINTS = 32;
+constexpr int HINTS = 256;            // per-SM claim hints (SM ids are below 256)
+constexpr int LINE_U64 = 16;          // one 128-byte line of u64 words
+constexpr int LINE_U32 = 32;          // ... of u32 words
 constexpr u32 CLS_LARGE = 0xFE;       // first page of an allocated large run
 constexpr u32 CLS_FREE_RUN = 0xFD;    // first page of a free large run
 constexpr u64 LOCK_WAIT_NS = 2000000000ull;
@@ -54,7 +56,7 @@ static_assert(sizeof(PageMeta) % 8 == 0 && offsetof(PageMeta, bits) % 8 == 0, "6
 static __device__ void push_partial(Heap* h, int c, u32 p) {
     PageMeta* pm = &h->meta[p];
     if (atomicCAS(&pm->listed, 0u, 1u) != 0u) return;
-    u64* head = &h->partial[c];
+    u64* head = &h->partial[c * LINE_U64];
     u64 old = *(volatile u64*)head;
     for (;;) {
         *(volatile u32*)&pm->pnext = (u32)(old & 0xffffffffull);
@@ -67,7 +69,7 @@ static __device__ void push_partial(Heap* h, int c, u32 p) {
 }
 
 static __device__ u32 pop_partial(Heap* h, int c) {
-    u64* head = &h->partial[c];
+    u64* head = &h->partial[c * LINE_U64];
     u64 old = *(volatile u64*)head;
     while ((old & 0xffffffffull) != 0) {
         const u32 cand = (u32)(old & 0xffffffffull) - 1;
@@ -153,7 +155,7 @@ static __device__ bool claim_in_page(Heap* h, u32 p, int c, int want, int rot, i
 static __device__ bool claim_batch(Heap* h, int c, int want, u32* page, int* w, u64* m) {
     const int stripe = (int)(smid() % HINTS);
     u32* hint = &h->cls_hint[c * HINTS + stripe];
-    const u32 n = *(volatile u32*)&h->cls_count[c];
+    const u32 n = *(volatile u32*)&h->cls_count[c * LINE_U32];
     const u32* list = h->cls_pages + (u64)c * h->npages;
     if (n > 0) {
         u32 start = *(volatile u32*)hint % n;
@@ -198,7 +200,7 @@ static __device__ bool claim_batch(Heap* h, int c, int want, u32* page, int* w, 
     u32 left = 0;
     if (!claim_in_page(h, p, c, want, 0, w, m, &left)) return false;
     __threadfence();
-    u32 slot = atomicAdd(&h->cls_count[c], 1u);
+    u32 slot = atomicAdd(&h->cls_count[c * LINE_U32], 1u);
     h->meta[p].slot = slot;
     __threadfence();
     if (slot < h->npages) {
@@ -424,13 +426,18 @@ __device__ u64 heap_usable_size(Heap* h, void* ptr) {
 // bump pointer, the free-run list head and lock, and the statistics
 // (1 frees of foreign pointers, 2 lock waits that ran out, 3 fresh small
 // pages, 4 partial-stack pops, 5 pops that found the page full).
+// Control words of a heap.  Every word that many threads update atomically
+// (each class's partial-stack head and page count, the bump pointer, the
+// large-run lock and list head, the counters) has a 128-byte line of its own,
+// so that atomics on one do not queue behind atomics on another.
+constexpr size_t LINE = 128;
 constexpr size_t CTL_PARTIAL = 0;
-constexpr size_t CTL_COUNT = CTL_PARTIAL + sizeof(u64) * NCLS;
-constexpr size_t CTL_HINT = CTL_COUNT + sizeof(u32) * NCLS;
-constexpr size_t CTL_NEXT = CTL_HINT + sizeof(u32) * NCLS * HINTS;
-constexpr size_t CTL_LARGE_HEAD = CTL_NEXT + sizeof(u32);
-constexpr size_t CTL_LARGE_LOCK = CTL_LARGE_HEAD + sizeof(u32);
-constexpr size_t CTL_STATS = CTL_LARGE_LOCK + sizeof(u32);
+constexpr size_t CTL_COUNT = CTL_PARTIAL + LINE * NCLS;
+constexpr size_t CTL_HINT = CTL_COUNT + LINE * NCLS;
+constexpr size_t CTL_NEXT = CTL_HINT + ((sizeof(u32) * NCLS * HINTS + LINE - 1) / LINE) * LINE;
+constexpr size_t CTL_LARGE_HEAD = CTL_NEXT + LINE;
+constexpr size_t CTL_LARGE_LOCK = CTL_LARGE_HEAD + LINE;
+constexpr size_t CTL_STATS = CTL_LARGE_LOCK + LINE;
 constexpr size_t CTL_BYTES = (CTL_STATS + sizeof(u32) * 8 + 255) & ~(size_t)255;
 
 __host__ size_t heap_ctl_bytes() { return CTL_BYTES; }

@@ -51,10 +51,11 @@ std::string shape_key(const gpumpi_coll_desc& d) {
 
 std::vector<int> algos_of(int op) {
     switch (op) {
+        case GPUMPI_COLL_BCAST: return {1, 2};
         case GPUMPI_COLL_REDUCE: return {1, 2};
-        case GPUMPI_COLL_ALLREDUCE:
+        case GPUMPI_COLL_ALLREDUCE: return {1, 2, 3};
         case GPUMPI_COLL_ALLTOALL:
-        case GPUMPI_COLL_ALLGATHER: return {1, 2, 3};
+        case GPUMPI_COLL_ALLGATHER: return {1, 2, 3, 4};
         default: return {0};
     }
 }

@@ -180,12 +180,17 @@ typedef struct gpumpi_comm_s* gpumpi_comm_t;
  * arrays of nranks device pointers (rank r's buffers).  count is elements per
  * rank: the broadcast length, the reduction length, or for ALLTOALL the block
  * sent to each peer.  algo selects the schedule (0 = by message size):
+ *   BCAST      1 every rank copies from the root, 2 binomial tree (log2 P
+ *              rounds, each rank copies from its parent once the parent has
+ *              its copy; always with flag rounds)
  *   REDUCE     1 root folds all inputs, 2 every rank folds a segment
  *   ALLREDUCE  1 every rank folds all inputs, 2 reduce-scatter + allgather,
  *              3 every rank folds its segment and writes it to every rank
  *   ALLTOALL, ALLGATHER  1 peer blocks one after another by the whole rank
  *              block, 2 one peer block per warp, 3 all peer blocks through
- *              one bulk asynchronous copy pipeline (cp.async.bulk)
+ *              one bulk asynchronous copy pipeline (cp.async.bulk), 4 the
+ *              16-byte vectors of all peer blocks spread over every thread
+ *              (launch-ordered plans; elsewhere as 0)
  * gpumpi_autotune fills it in, and `sync` in the batched form. */
 typedef struct gpumpi_coll_desc {
     gpumpi_comm_t comm;

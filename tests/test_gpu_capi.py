@@ -35,11 +35,11 @@ def _rank_fold(xs, op):
     return acc
 
 
-@pytest.mark.parametrize("algo", [0, 1, 2, 3])
+@pytest.mark.parametrize("algo", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("form", ["plain", "batched", "graph", "plain-flags", "graph-flags", "graph-mixed"])
 @pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (32, 1 << 16)])
 def test_capi_collectives(coll, form, nranks, count, algo):
-    """Every schedule (algo 1-3 and the size-based choice 0) folds in rank
+    """Every schedule (algo 1-4 and the size-based choice 0) folds in rank
     order, so each gives the host fold's bits, in the launch-ordered forms
     (the calls are independent), with flag rounds (-flags) and with both in
     one launch (-mixed)."""
@@ -173,7 +173,7 @@ def test_autotune_picks_valid_schedules_and_keeps_results(coll, tmp_path):
     bt, plain, palgos = mod.autotune(lib, descs, reps=3, cache_path=cache)
     assert bt in (64, 128, 256, 512, 1024)
     assert all(t in (64, 128, 256, 512, 1024) for t in plain)
-    assert all(d.algo in (1, 2, 3) for d in descs) and all(a in (1, 2, 3) for a in palgos)
+    assert all(d.algo in (1, 2, 3, 4) for d in descs) and all(a in (1, 2, 3, 4) for a in palgos)
     lines = open(cache).read().splitlines()
     assert len(descs) <= len(lines) <= 5 * len(descs)
     # a second run reads the plain results from the cache and returns the same plain choices

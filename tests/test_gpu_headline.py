@@ -85,11 +85,12 @@ def test_headline_plan_tuned_bitwise_2_17(env):
     _run_checked(bench, coll, lib, 17)
 
 
-@pytest.mark.parametrize("algo", [1, 2, 3])
+@pytest.mark.parametrize("algo", [1, 2, 3, 4])
 def test_headline_plan_each_schedule_bitwise_2_17(env, algo):
-    """algo 1/2/3 for every call: Allreduce every-rank fold / reduce-scatter +
-    allgather / pushing bulk-staged fold; Alltoall whole-block / per-warp /
-    bulk engine (Bcast has one schedule)."""
+    """algo 1/2/3/4 for every call: Allreduce every-rank fold / reduce-scatter
+    + allgather / pushing bulk-staged fold (and 4 as 3); Alltoall whole-block /
+    per-warp / bulk engine / vectors of all blocks over all threads; Bcast
+    from the root / binomial tree (and 3, 4 as 1)."""
     bench, coll, lib = env
     _run_checked(bench, coll, lib, 17, algo=algo)
 
