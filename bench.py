@@ -700,6 +700,17 @@ def main():
         eplans.append(eplan)
         eparts.append((eplan, hs, hr, torch.cuda.Stream(), (gkeep, gitems, hsend, hrecv)))
     ebytes = alg_bytes(COMM_SIZES, ne)
+    # the copy bandwidth of the end-to-end leg's own pinned buffers (host
+    # memory placement varies between boxes and runs)
+    probe = eparts[0][4][2]
+    pd = torch.empty(probe.numel(), dtype=torch.uint8, device="cuda")
+    pd.copy_(probe, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pd.copy_(probe, non_blocking=True)
+    torch.cuda.synchronize()
+    buf_h2d = probe.numel() / (time.perf_counter() - t0) / 1e9
+    del pd
 
     def e2e_step():
         h2d = d2h = 0
@@ -805,7 +816,7 @@ def main():
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "elements_per_rank": ne,
                     "seconds_per_step": round(esecs / e_steps, 5), "plans_only_seconds_per_step": round(ekern, 5),
-                    "host_link_GBps": link,
+                    "host_link_GBps": link, "e2e_buffer_h2d_GBps": round(buf_h2d, 1),
                     "form": "gpumpi_plan_run_host, the 16 communicators as 4 batched plans on 4 streams"},
             "sustained": sustained,
             "sweep": sweep,
