@@ -451,8 +451,10 @@ static __device__ __forceinline__ void fold_bulk_issue(const char* src, u32 len,
 template <class T, class O>
 static __device__ __noinline__ int fold_push_bulk_t(const char* const* ptab, const char* const* otab, int nin, u64 lo,
                                                     u64 nvec, int tid, int T_, char* ring, u64* bars, int ns) {
-    const u32 C = (u32)T_ * 16;
-    const u64 K = (nvec + T_ - 1) / T_ * (u64)nin;
+    // vectors per stage: one per thread, or every vector of a short segment
+    const u32 VPS = nvec < (u64)T_ ? (u32)nvec : (u32)T_;
+    const u32 C = VPS * 16;
+    const u64 K = (nvec + VPS - 1) / VPS * (u64)nin;
     const u64 off = lo * sizeof(T);
     const u32 ring_s = (u32)__cvta_generic_to_shared(ring);
     const u32 full_s = (u32)__cvta_generic_to_shared(bars);   // full[0..ns), then empty[0..ns)
@@ -463,13 +465,13 @@ static __device__ __noinline__ int fold_push_bulk_t(const char* const* ptab, con
     int iq = 0, ist = 0;
 #define GM_FOLD_ISSUE()                                                                                \
     do {                                                                                               \
-        const u64 nv_ = nvec - iv0 < (u64)T_ ? nvec - iv0 : (u64)T_;                                   \
+        const u64 nv_ = nvec - iv0 < (u64)VPS ? nvec - iv0 : (u64)VPS;                                 \
         fold_bulk_issue(ptab[iq] + off + iv0 * 16, (u32)(nv_ * 16), ring_s + (u32)ist * C,             \
                         full_s + 8u * (u32)ist);                                                       \
         issued++;                                                                                      \
         if (++iq == nin) {                                                                             \
             iq = 0;                                                                                    \
-            iv0 += (u64)T_;                                                                            \
+            iv0 += (u64)VPS;                                                                           \
         }                                                                                              \
         if (++ist == ns) ist = 0;                                                                      \
     } while (0)
@@ -507,7 +509,7 @@ static __device__ __noinline__ int fold_push_bulk_t(const char* const* ptab, con
             if (v < nvec)
                 for (int r = 0; r < nin; r++) reinterpret_cast<uint4*>(const_cast<char*>(otab[r]) + off)[v] = acc;
             q = 0;
-            v += (u64)T_;
+            v += (u64)VPS;
         }
     }
 #undef GM_FOLD_ISSUE
@@ -587,10 +589,10 @@ __device__ bool fold_range_push(int opi, MPI_Datatype base, const Pub* pub, int 
     const u64 esz = basic_info((int)base).size;
     const u64 nvec = hi > lo ? (hi - lo) * esz / 16 : 0;
     const u32 tab_bytes = (u32)(2 * nin * sizeof(char*));
-    const u32 C = (u32)T_ * 16;
+    const u32 C = (nvec < (u64)T_ ? (u32)nvec : (u32)T_) * 16;   // a stage: one vector per thread at most
     const u32 avail = bulk_stage_bytes();
     int ns = 0;
-    if (!bctx().bulk_broken && nvec >= (u64)T_ && avail > tab_bytes + 256) {
+    if (!bctx().bulk_broken && nvec >= 16 && avail > tab_bytes + 256) {
         ns = (int)((avail - tab_bytes - 256) / C);
         if (ns > 16) ns = 16;
     }

@@ -37,7 +37,7 @@ def _rank_fold(xs, op):
 
 @pytest.mark.parametrize("algo", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("form", ["plain", "batched", "graph", "plain-flags", "graph-flags", "graph-mixed"])
-@pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (32, 1 << 16)])
+@pytest.mark.parametrize("nranks,count", [(1, 5), (4, 1000), (7, 4097), (64, 1 << 12), (32, 1 << 16)])
 def test_capi_collectives(coll, form, nranks, count, algo):
     """Every schedule (algo 1-4 and the size-based choice 0) folds in rank
     order, so each gives the host fold's bits, in the launch-ordered forms
