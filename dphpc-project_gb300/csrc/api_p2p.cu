@@ -8,6 +8,7 @@
 // memory; the reference instead copied non-global buffers into malloc'd bounce
 // buffers (gpu_libs/gpu_libc/cuda_mpi.cu:183-194).
 #include "rt.cuh"
+#include "p2p_small.cuh"
 
 using namespace gm;
 
@@ -220,9 +221,10 @@ __device__ int MPI_Get_count(const MPI_Status* status, MPI_Datatype datatype, in
 // ---------------------------------------------------------------- point to point
 // A blocking send or receive of an eager message with a basic type, valid
 // arguments and no posted receive or deferred send takes the leader-only path
-// without a request object (p2p_send_small and p2p_recv_small decide by size
-// and buffer).  Anything else, and a full mailbox, goes through the request
-// path, which also reports argument errors.
+// without a request object (leader_send and recv_small decide by size and
+// buffer; a message of at most INLINE_BYTES travels in its header and is sent
+// and taken inline here).  Anything else, and a full mailbox, goes through the
+// request path, which also reports argument errors.
 
 // The communicator of a leader-path call: context, the caller's rank, size
 // and member table (nullptr: ranks are job ranks).  MPI_COMM_WORLD comes from
@@ -262,8 +264,19 @@ static __device__ __forceinline__ bool small_call(const BlockCtx& b, MPI_Comm co
         w.sc_size = sc->size;
         w.sc_members = sc->members;
     }
-    *bytes = (u64)count * (u64)dtype_size(datatype);
+    *bytes = (u64)count * (u64)basic_size((int)datatype);
     return true;
+}
+
+// Leader: blocking eager send (rendezvous above the eager size is the
+// caller's); 1 when sent (*rc), 0 when the request path must take it.
+static __device__ __forceinline__ int leader_send(const void* buf, u64 bytes, int dj, int ctx, int me, int tag,
+                                                  int* rc) {
+    if (bytes <= INLINE_BYTES) {
+        *rc = MPI_SUCCESS;
+        return send_tiny(buf, (u32)bytes, dj, ctx, me, tag);
+    }
+    return p2p_send_small(buf, bytes, dj, ctx, me, tag, rc);
 }
 
 static __device__ int start_send(const void* buf, int count, MPI_Datatype datatype, int dest,
@@ -657,7 +670,7 @@ __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int d
             const int dj = sc.job_rank(dest);
             // the blocking rendezvous waits without progressing lazy receives:
             // with some pending, MPI_Wait on an MPI_Isend request waits instead
-            if (bytes <= b.eager_bytes ? p2p_send_small(buf, bytes, dj, sc.ctx, sc.me, tag, &rc)
+            if (bytes <= b.eager_bytes ? leader_send(buf, bytes, dj, sc.ctx, sc.me, tag, &rc)
                                        : b.lazy_n == 0 && p2p_send_rdv_small(buf, bytes, dj, sc.ctx, sc.me, tag, &rc))
                 return rc;
         }
@@ -684,7 +697,7 @@ __device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source,
             (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
             int rc = MPI_SUCCESS;
-            if (p2p_recv_small(buf, bytes, sc.ctx, source, tag, status, &rc)) return rc;
+            if (recv_small(buf, bytes, sc.ctx, source, tag, status, &rc)) return rc;
         }
     }
     MPI_Request r = MPI_REQUEST_NULL;
@@ -710,7 +723,7 @@ __device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sen
             (recvtag == MPI_ANY_TAG || (recvtag >= 0 && recvtag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
             int rc = MPI_SUCCESS;
-            if (p2p_send_small(sendbuf, sbytes, sc.job_rank(dest), sc.ctx, sc.me, sendtag, &rc)) {
+            if (leader_send(sendbuf, sbytes, sc.job_rank(dest), sc.ctx, sc.me, sendtag, &rc)) {
                 if (rc) return rc;
                 return MPI_Recv(recvbuf, recvcount, recvtype, source, recvtag, comm, status);
             }

@@ -42,7 +42,8 @@ struct TypeInfo {
     int cls;
 };
 
-static __device__ TypeInfo basic_info(int t) {
+// Element kind and class of basic datatype t (the size field is filled by basic_info).
+static __device__ TypeInfo basic_kind(int t) {
     switch (t) {
         case MPI_CHAR: return {1, K_OPAQUE1, TC_TEXT};
         case MPI_SHORT: return {2, K_I16, TC_INT};
@@ -81,6 +82,13 @@ static __device__ TypeInfo basic_info(int t) {
         case MPI_PACKED: return {1, K_OPAQUE1, TC_BYTE};
         default: return {-1, K_BAD, TC_BAD};
     }
+}
+
+// Size (from the datatype list's C types), element kind and class of basic datatype t.
+static __device__ TypeInfo basic_info(int t) {
+    TypeInfo ti = basic_kind(t);
+    if (ti.canon != K_BAD) ti.size = basic_size(t);
+    return ti;
 }
 
 __device__ int dtype_base(MPI_Datatype t, int* mult) {

@@ -25,6 +25,7 @@
 //    stamp is always the oldest message of that sender;
 //  * every wait is bounded and returns an error code instead of spinning forever.
 #include "rt.cuh"
+#include "p2p_small.cuh"
 
 namespace gm {
 
@@ -520,6 +521,7 @@ __device__ int rdv_wait_leader(MPI_Request_impl* r) {
         const int rc = lazy_progress();
         if (rc) return rc;
         if (!b.p2p_quiet) return MPI_SUCCESS;   // block path receives posted: wait there
+        mb_release_taken();
         if (ld_relaxed_int(&j->status[0]) != 0) return fail_code(j);
         if (gtime() - t0 > b.timeout_ns) {
             job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
@@ -545,29 +547,6 @@ static __device__ bool leader_bulk_ok(const void* p, u64 n) {
            bulk_stage_bytes() >= 8192;
 }
 
-// Leader: claim a free slot of mailbox mb (first guess from the bits last seen
-// there), or -1 when it is full.
-static __device__ int claim_slot_small(Mailbox* mb) {
-    BlockCtx& b = bctx();
-    u64 used = b.slot_hint;
-    for (int tries = 0;; tries++) {
-        if (~used == 0) {
-            if (tries) return -1;
-            used = mb_ld(&mb->used);
-            if (~used == 0) return -1;
-        }
-        const int s = __ffsll((long long)~used) - 1;
-        const u64 bit = 1ull << s;
-        // acquire: the slot is written only after the receiver released it
-        const u64 old = mb_atom_or_acquire(&mb->used, bit);   // the bit's 32-bit half
-        if (!(old & bit)) {
-            b.slot_hint = (used & ((bit >> 32) ? 0xffffffffull : ~0xffffffffull)) | old | bit;
-            return s;
-        }
-        used |= old | bit;
-    }
-}
-
 // Leader: blocking rendezvous send without a request object.
 // The header points the receiver at the user's (global) buffer and at the
 // rank's completion word; the call returns once the receiver has copied the
@@ -591,6 +570,7 @@ __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int 
     const u64 t0 = gtime();
     unsigned ns = 32;
     while (!ld_acquire32(done)) {
+        mb_release_taken();
         if (ld_relaxed_int(&j->status[0]) != 0) {
             *rc = fail_code(j);
             return 1;
@@ -613,6 +593,10 @@ __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int 
 // the destination's mailbox is full.
 __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc) {
     BlockCtx& b = bctx();
+    if (bytes <= INLINE_BYTES) {   // the payload travels in the header
+        *rc = MPI_SUCCESS;
+        return send_tiny(buf, (u32)bytes, dest_job, ctx, me, tag);
+    }
     const bool bulk = leader_bulk_ok(buf, bytes);
     if (bytes > FAST_MSG_BYTES && !bulk) return 0;
     Mailbox* mb = mbox_of(dest_job);
@@ -632,16 +616,7 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx,
     *(ulonglong2*)&h->bytes = make_ulonglong2(bytes, stamp);
     char* slot = b.eager + ((u64)dest_job * MB_SLOTS + s) * b.eager_bytes;
     *rc = MPI_SUCCESS;
-    if (bytes <= INLINE_BYTES) {   // the payload travels in the header
-        unsigned char tmp[INLINE_BYTES];
-        if (pre) {
-            memcpy(tmp, &v[0], INLINE_BYTES);
-        } else {
-            for (u64 i = 0; i < bytes; i++) tmp[i] = ((const unsigned char*)buf)[i];
-            for (u64 i = bytes; i < INLINE_BYTES; i++) tmp[i] = 0;
-        }
-        *(uint4*)&h->inl = *(const uint4*)tmp;
-    } else if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
+    if (pre) {   // whole vectors: the slot holds at least 16 * ceil(bytes / 16) bytes
 #pragma unroll
         for (int k = 0; k < 4; k++)
             if ((u64)k * 16 < bytes) ((uint4*)slot)[k] = v[k];
@@ -658,49 +633,12 @@ __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx,
 }
 
 // ---------------------------------------------------------------- leader receives
-// A message of this rank's mailbox that matched (ctx, source, tag).
-struct SmallMatch {
-    int slot, src, tag, kind;
-    u64 bytes;
-    uint4 pre;   // the payload of an eager message of at most INLINE_BYTES
-};
-
-// The oldest message among the `ready` slots matching (ctx, source, tag).  The
-// header's first 32 bytes are read as two vectors, the first 16 payload bytes
-// with them.
-static __device__ bool small_match(Mailbox* mb, const char* slots, u64 ready, int ctx, int source, int tag,
-                                   SmallMatch* m) {
+// Receive matched message m into buf (capacity `bytes`) and take its slot
+// (released at the leader's next idle moment, mb_take).  Returns 1 (done: *rc
+// and *got set), or 0 when the request path must take it (nothing consumed).
+__device__ int p2p_small_take(Mailbox* mb, const SmallMatch& m, void* buf, u64 bytes, int* rc, u64* got) {
     BlockCtx& b = bctx();
-    u64 best_stamp = ~0ull;
-    m->slot = -1;
-    while (ready) {
-        const int s = __ffsll((long long)ready) - 1;
-        ready &= ready - 1;
-        const int4 h0 = mb_ld4(&mb->hdr[s]);
-        const ulonglong2 h1 = mb_ld2(&mb->hdr[s].bytes);
-        const ulonglong2 p0 = mb_ld2(&mb->hdr[s].inl);   // the payload when bytes <= INLINE_BYTES
-        if (h0.x != ctx) continue;
-        if (source != MPI_ANY_SOURCE && h0.y != source) continue;
-        if (tag != MPI_ANY_TAG && h0.z != tag) continue;
-        if (h1.y < best_stamp) {
-            best_stamp = h1.y;
-            m->slot = s;
-            m->src = h0.y;
-            m->tag = h0.z;
-            m->kind = h0.w;
-            m->bytes = h1.x;
-            m->pre = *(const uint4*)&p0;
-        }
-    }
-    return m->slot >= 0;
-}
-
-// Receive matched message m into buf (capacity `bytes`) and release its slot.
-// Returns 1 (done: *rc and *got set), or 0 when the request path must take it
-// (nothing consumed).
-static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatch& m, void* buf, u64 bytes,
-                                 int* rc, u64* got) {
-    BlockCtx& b = bctx();
+    const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
     const u64 n = m.bytes < bytes ? m.bytes : bytes;
     const bool bulk = leader_bulk_ok(buf, n);
     u32* rdv_done = nullptr;
@@ -716,13 +654,9 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
     }
     char* d = (char*)buf;
     *got = 0;
-    if (!bulk && m.kind == 0 && m.bytes <= INLINE_BYTES) {
-        // the payload is already in registers: free the slot first, so that
-        // the release waits for no store, then write the user's buffer
-        mb_red_and_relaxed(&mb->ready, ~(1ull << m.slot));
-        mb_red_and_release(&mb->used, ~(1ull << m.slot));
-        const char* pc = (const char*)&m.pre;
-        for (u64 i = 0; i < n; i++) d[i] = pc[i];
+    if (m.kind == 0 && m.bytes <= INLINE_BYTES) {   // the payload is already in registers
+        mb_take(mb, m.slot);
+        tiny_store(d, m.pre, (u32)n);
         *rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
         *got = n;
         return 1;
@@ -733,9 +667,6 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
         *rc = leader_bulk_copy(d, src, n16);
         if (*rc) return 1;   // the job has failed; the slot stays claimed
         for (u64 i = n16; i < n; i++) d[i] = __ldcg(src + i);
-    } else if (m.bytes <= INLINE_BYTES) {
-        const char* pc = (const char*)&m.pre;
-        for (u64 i = 0; i < n; i++) d[i] = pc[i];
     } else {
         const char* src = slots + (u64)m.slot * b.eager_bytes;
         u64 i = 0;
@@ -747,57 +678,26 @@ static __device__ int small_take(Mailbox* mb, const char* slots, const SmallMatc
         }
         for (; i < n; i++) d[i] = __ldcg(src + i);
     }
-    mb_red_and_relaxed(&mb->ready, ~(1ull << m.slot));
     if (rdv_done) {
         __threadfence();
         st_release32(rdv_done, 1u);
     }
-    mb_red_and_release(&mb->used, ~(1ull << m.slot));
+    mb_take(mb, m.slot);
     *rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
     *got = n;
     return 1;
 }
 
-// Leader: blocking receive without a request object.
-__device__ int p2p_recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st, int* rc) {
-    BlockCtx& b = bctx();
-    Job* j = b.job;
-    Mailbox* mb = mbox_of(b.rank);
-    const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
-    const u64 t0 = gtime();
-    unsigned ns = 32;
-    for (unsigned it = 0;; it++) {
-        // acquire on every poll: nothing read after it comes from L1 anyway
-        const u64 ready = mb_ld_acquire(&mb->ready);
-        SmallMatch m;
-        if (ready && small_match(mb, slots, ready, ctx, source, tag, &m)) {
-            u64 got = 0;
-            if (!small_take(mb, slots, m, buf, bytes, rc, &got)) return 0;
-            if (st) {
-                st->MPI_SOURCE = m.src;
-                st->MPI_TAG = m.tag;
-                st->MPI_ERROR = *rc;
-                st->gpumpi_count_lo = (int)(got & 0xffffffffu);
-                st->gpumpi_count_hi = (int)(got >> 32);
-            }
-            return 1;
-        }
-        // the abort word and the clock every 8th poll: a poll of a mailbox in
-        // shared memory is much shorter than a load of the abort word
-        if ((it & 7u) == 7u) {
-            if (ld_relaxed_int(&j->status[0]) != 0) {
-                *rc = fail_code(j);
-                return 1;
-            }
-            if (gtime() - t0 > b.timeout_ns) {
-                job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
-                *rc = GPUMPI_ERR_TIMEOUT;
-                return 1;
-            }
-        }
-        __nanosleep(ns);
-        if (ns < 128) ns <<= 1;
-    }
+// Payloads of at most INLINE_BYTES that are not one aligned access.
+__device__ ulonglong2 tiny_load_bytes(const void* buf, u32 n) {
+    ulonglong2 w = make_ulonglong2(0ull, 0ull);
+    unsigned char* t = reinterpret_cast<unsigned char*>(&w);
+    for (u32 i = 0; i < n && i < INLINE_BYTES; i++) t[i] = ((const unsigned char*)buf)[i];
+    return w;
+}
+__device__ void tiny_store_bytes(void* buf, ulonglong2 w, u32 n) {
+    const unsigned char* t = reinterpret_cast<const unsigned char*>(&w);
+    for (u32 i = 0; i < n && i < INLINE_BYTES; i++) ((unsigned char*)buf)[i] = t[i];
 }
 
 // ---------------------------------------------------------------- lazy receives
@@ -848,20 +748,19 @@ __device__ int lazy_progress() {
     BlockCtx& b = bctx();
     if (b.lazy_n == 0) return MPI_SUCCESS;
     Mailbox* mb = mbox_of(b.rank);
-    const char* slots = b.eager + (u64)b.rank * MB_SLOTS * b.eager_bytes;
     u64 ready = mb_ld_acquire(&mb->ready);
     RankPriv* p = b.priv;
     int i = 0;
     while (i < b.lazy_n && ready) {
         MPI_Request_impl* r = &p->reqs[b.lazy[i]];
         SmallMatch m;
-        if (!small_match(mb, slots, ready, r->ctx, r->peer, r->tag, &m)) {
+        if (!small_match(mb, ready, r->ctx, r->peer, r->tag, &m)) {
             i++;
             continue;
         }
         int rc = MPI_SUCCESS;
         u64 got = 0;
-        if (!small_take(mb, slots, m, r->buf, r->bytes, &rc, &got)) return lazy_materialize();
+        if (!p2p_small_take(mb, m, r->buf, r->bytes, &rc, &got)) return lazy_materialize();
         ready &= ~(1ull << m.slot);
         r->st_source = m.src;
         r->st_tag = m.tag;
@@ -888,6 +787,7 @@ __device__ int lazy_wait(MPI_Request_impl* r) {
         if (r->state != RS_LAZY) return MPI_SUCCESS;
         // a deferred send needs the block path's progress: wait there
         if (!b.p2p_quiet) return lazy_materialize();
+        mb_release_taken();
         if (ld_relaxed_int(&j->status[0]) != 0) return fail_code(j);
         if (gtime() - t0 > b.timeout_ns) {
             job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
@@ -953,12 +853,12 @@ __device__ int p2p_recv_fast(MPI_Request_impl* r, int* handled) {
             r->st_tag = h0.z;
             r->st_bytes = n;
             r->st_err = bytes > r->bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
-            mb_red_and_relaxed(&mb->ready, ~(1ull << best));
-            mb_red_and_release(&mb->used, ~(1ull << best));
+            mb_take(mb, best);
             r->state = RS_DONE;
             *handled = 1;
             return MPI_SUCCESS;
         }
+        mb_release_taken();
         if (job_aborted(j)) return fail_code(j);
         if (gtime() - t0 > j->timeout_ns) {
             job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");

@@ -564,6 +564,8 @@ struct BlockCtx {
     u64 eager_bytes;
     u64 timeout_ns;
     u64 slot_hint;                // `used` bits last seen at a destination
+    u64 mb_taken;                 // slots of the own mailbox whose messages the leader took
+                                  // and whose release waits for its next idle moment
     int world_ctx, world_size;
     int p2p_quiet;                // no posted receive and no deferred send
     unsigned api_calls;           // counts calls between checks of the abort word
@@ -708,6 +710,41 @@ __device__ __forceinline__ void mb_red_and_release(u64* p, u64 mask) {
         asm volatile("red.release.gpu.and.b32 [%0], %1;" ::"l"(mb_half(p, bit)), "r"(~mb_bit32(bit)) : "memory");
 }
 
+// Clear several bits of a slot mask, release (one 32-bit atomic per half that has bits).
+__device__ __forceinline__ void mb_release_bits(u64* p, u64 bits) {
+    u32* w = reinterpret_cast<u32*>(p);
+    const u32 lo = (u32)bits, hi = (u32)(bits >> 32);
+    if (mb_in_cluster()) {
+        if (lo) asm volatile("red.release.cluster.and.b32 [%0], %1;" ::"l"(w), "r"(~lo) : "memory");
+        if (hi) asm volatile("red.release.cluster.and.b32 [%0], %1;" ::"l"(w + 1), "r"(~hi) : "memory");
+    } else {
+        if (lo) asm volatile("red.release.gpu.and.b32 [%0], %1;" ::"l"(w), "r"(~lo) : "memory");
+        if (hi) asm volatile("red.release.gpu.and.b32 [%0], %1;" ::"l"(w + 1), "r"(~hi) : "memory");
+    }
+}
+
+// Slots of the leader's own mailbox.  A message the leader takes has its
+// ready bit cleared at once (relaxed: the slot stays claimed), while the
+// release of the slot itself -- a release operation, whose fence would wait
+// for every earlier memory operation of the thread -- is put off until the
+// leader next waits (mb_release_taken: on a poll that finds nothing, before a
+// block-path call, or once MB_TAKEN_MAX slots are held), off the path between
+// a message's arrival and the caller's next operation.
+constexpr int MB_TAKEN_MAX = 16;
+__device__ __forceinline__ void mb_release_taken() {
+    BlockCtx& b = bctx();
+    if (b.mb_taken) {
+        mb_release_bits(&mbox_of(b.rank)->used, b.mb_taken);
+        b.mb_taken = 0;
+    }
+}
+__device__ __forceinline__ void mb_take(Mailbox* mb, int s) {
+    BlockCtx& b = bctx();
+    mb_red_and_relaxed(&mb->ready, ~(1ull << s));
+    b.mb_taken |= 1ull << s;
+    if (__popcll(b.mb_taken) >= MB_TAKEN_MAX) mb_release_taken();
+}
+
 // Intra-call barrier of all threads of the rank block.
 __device__ __forceinline__ void bsync() { bar_named(2, bctx().T); }
 
@@ -783,6 +820,38 @@ __device__ __forceinline__ int comm_world_rank(const MPI_Comm_impl* c, int r) {
 }
 
 // datatypes / operators
+// The size of every basic datatype, packed at compile time from the datatype
+// list (enum order) as 3-bit base-2 logarithms, so that a size is a shift of
+// a constant rather than a call or a table load.
+#define GPUMPI_SIZE_F(name, type) (unsigned)sizeof(type)
+#define GPUMPI_SIZE_SEP ,
+constexpr unsigned kBasicSizes[] = {GPUMPI_TYPES_LIST(GPUMPI_SIZE_F, GPUMPI_SIZE_SEP)};
+#undef GPUMPI_SIZE_F
+#undef GPUMPI_SIZE_SEP
+constexpr int kNumBasic = (int)(sizeof(kBasicSizes) / sizeof(kBasicSizes[0]));
+static_assert(kNumBasic == GPUMPI_NUM_BASIC_TYPES, "datatype list and enum differ");
+static_assert(kNumBasic <= 42, "two words of packed sizes");
+constexpr int size_lg2(unsigned v) { return v <= 1 ? 0 : 1 + size_lg2(v >> 1); }
+constexpr bool sizes_ok() {
+    for (int i = 0; i < kNumBasic; i++)
+        if (kBasicSizes[i] == 0 || (kBasicSizes[i] & (kBasicSizes[i] - 1)) != 0 || kBasicSizes[i] > 64) return false;
+    return true;
+}
+static_assert(sizes_ok(), "basic datatype sizes are powers of two up to 64 bytes");
+constexpr u64 pack_size_lg2(int from) {
+    u64 w = 0;
+    for (int i = 0; i < 21 && from + i < kNumBasic; i++) w |= (u64)size_lg2(kBasicSizes[from + i]) << (3 * i);
+    return w;
+}
+constexpr u64 kSizeLg2Lo = pack_size_lg2(0), kSizeLg2Hi = pack_size_lg2(21);
+
+// Size in bytes of basic datatype t, 0 <= t < GPUMPI_NUM_BASIC_TYPES.
+__device__ __forceinline__ int basic_size(int t) {
+    const bool lo = t < 21;
+    const u64 w = lo ? kSizeLg2Lo : kSizeLg2Hi;
+    return 1 << (int)((w >> (3 * (lo ? t : t - 21))) & 7);
+}
+
 __device__ int dtype_size(MPI_Datatype t);
 __device__ int dtype_base(MPI_Datatype t, int* mult);
 __device__ int op_check(MPI_Op op, MPI_Datatype t);
@@ -807,7 +876,6 @@ constexpr u64 SMALL_BULK_MIN = 512;    // leader copies from this size go throug
 // set), 0 when the request path must take the call.
 __device__ int p2p_send_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc);
 __device__ int p2p_send_rdv_small(const void* buf, u64 bytes, int dest_job, int ctx, int me, int tag, int* rc);
-__device__ int p2p_recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st, int* rc);
 __device__ int lazy_materialize();
 __device__ int lazy_progress();
 __device__ int lazy_wait(MPI_Request_impl* r);

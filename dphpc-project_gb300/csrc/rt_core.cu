@@ -304,6 +304,7 @@ __device__ void blk_memset(void* dst, int c, u64 n, int tid, int T) {
 // ---------------------------------------------------------------- call protocol
 __device__ int block_call(Call& c) {
     BlockCtx& b = bctx();
+    mb_release_taken();   // the block path may wait on senders that need those slots
     // Lazy receives go to the block path before any point-to-point call there:
     // it matches in posting order, and a wait on a rendezvous send needs the
     // receives it depends on to progress (two ranks in MPI_Sendrecv).
@@ -479,6 +480,7 @@ static __device__ void block_ctx_init(Job* job, int rank, int slot, u32 C, u32 c
     b.in_call = 0;
     b.bulk_broken = 0;
     b.lazy_n = 0;
+    b.mb_taken = 0;
     b.call.op = -1;
     b.cl_n = (int)C;
     b.cl_rank = (int)crank;
