@@ -236,10 +236,28 @@ struct SmallComm {
     __device__ __forceinline__ int job_rank(int r) const { return members ? __ldcg(&members[r]) : r; }
 };
 
-static __device__ __forceinline__ bool small_call(const BlockCtx& b, MPI_Comm comm, int count,
-                                                  MPI_Datatype datatype, u64* bytes, SmallComm* sc) {
-    if (!b.p2p_quiet || count < 0 || (int)datatype < 0 || (int)datatype >= GPUMPI_NUM_BASIC_TYPES)
-        return false;
+// Make `comm` the block's cached communicator; false when it is not a valid
+// handle (the request path then reports the error).
+static __device__ __noinline__ bool small_comm_cache(MPI_Comm comm) {
+    const MPI_Comm_impl* c = comm_resolve(comm);
+    if (!c) return false;
+    BlockCtx& b = bctx();
+    b.sc_handle = (const void*)comm;
+    b.sc_ctx = c->ctx;
+    b.sc_me = c->rank;
+    b.sc_size = c->size;
+    b.sc_members = c->cs->members;
+    return true;
+}
+
+// 1: the call may take the leader path (*bytes and *sc set); 0: it takes the
+// request path; SMALL_UNCACHED: comm is neither MPI_COMM_WORLD nor the cached
+// communicator, and the caller retries after small_comm_cache (through a call
+// in tail position, so that nothing stays live across it).
+constexpr int SMALL_UNCACHED = -1;
+static __device__ __forceinline__ int small_call(const BlockCtx& b, MPI_Comm comm, int count,
+                                                 MPI_Datatype datatype, u64* bytes, SmallComm* sc) {
+    if (!b.p2p_quiet || count < 0 || (int)datatype < 0 || (int)datatype >= GPUMPI_NUM_BASIC_TYPES) return 0;
     if (comm == &gm_world_sentinel) {
         sc->ctx = b.world_ctx;
         sc->me = b.rank;
@@ -251,32 +269,47 @@ static __device__ __forceinline__ bool small_call(const BlockCtx& b, MPI_Comm co
         sc->size = b.sc_size;
         sc->members = b.sc_members;
     } else {
-        const MPI_Comm_impl* c = comm_resolve(comm);
-        if (!c) return false;
-        sc->ctx = c->ctx;
-        sc->me = c->rank;
-        sc->size = c->size;
-        sc->members = c->cs->members;
-        BlockCtx& w = const_cast<BlockCtx&>(b);
-        w.sc_handle = (const void*)comm;
-        w.sc_ctx = sc->ctx;
-        w.sc_me = sc->me;
-        w.sc_size = sc->size;
-        w.sc_members = sc->members;
+        return SMALL_UNCACHED;
     }
     *bytes = (u64)count * (u64)basic_size((int)datatype);
-    return true;
+    return 1;
 }
 
-// Leader: blocking eager send (rendezvous above the eager size is the
-// caller's); 1 when sent (*rc), 0 when the request path must take it.
-static __device__ __forceinline__ int leader_send(const void* buf, u64 bytes, int dj, int ctx, int me, int tag,
-                                                  int* rc) {
-    if (bytes <= INLINE_BYTES) {
-        *rc = MPI_SUCCESS;
-        return send_tiny(buf, (u32)bytes, dj, ctx, me, tag);
-    }
-    return p2p_send_small(buf, bytes, dj, ctx, me, tag, rc);
+// Leader: blocking send of a message above INLINE_BYTES without a request
+// object (eager up to the eager size, else rendezvous while no lazy receive is
+// pending: the blocking rendezvous waits without progressing them, so with
+// some pending MPI_Wait on an MPI_Isend request waits instead).  Returns the
+// MPI result, or LEADER_PASS when the request path must take the message.  Out of line,
+// like the other paths of the blocking calls below, so that the inline path of
+// a message of a few bytes saves and restores only the registers it uses.
+static __device__ __noinline__ int leader_send_large(const void* buf, u64 bytes, int dj, int ctx, int me, int tag) {
+    BlockCtx& b = bctx();
+    int rc = MPI_SUCCESS;
+    if (bytes <= b.eager_bytes ? p2p_send_small(buf, bytes, dj, ctx, me, tag, &rc)
+                               : b.lazy_n == 0 && p2p_send_rdv_small(buf, bytes, dj, ctx, me, tag, &rc))
+        return rc;
+    return LEADER_PASS;
+}
+
+// Leader: blocking eager or rendezvous send; the MPI result, or LEADER_PASS
+// when the request path must take the message.
+static __device__ __forceinline__ int leader_send(const void* buf, u64 bytes, int dj, int ctx, int me, int tag) {
+    if (bytes <= INLINE_BYTES) return send_tiny(buf, (u32)bytes, dj, ctx, me, tag) ? MPI_SUCCESS : LEADER_PASS;
+    return leader_send_large(buf, bytes, dj, ctx, me, tag);
+}
+
+static __device__ __noinline__ int send_request_path(const void* buf, int count, MPI_Datatype datatype, int dest,
+                                                     int tag, MPI_Comm comm) {
+    MPI_Request r = MPI_REQUEST_NULL;
+    int rc = MPI_Isend(buf, count, datatype, dest, tag, comm, &r);
+    if (rc) return rc;
+    return MPI_Wait(&r, MPI_STATUS_IGNORE);
+}
+
+static __device__ __noinline__ int send_uncached(const void* buf, int count, MPI_Datatype datatype, int dest,
+                                                 int tag, MPI_Comm comm) {
+    if (!small_comm_cache(comm)) return send_request_path(buf, count, datatype, dest, tag, comm);
+    return MPI_Send(buf, count, datatype, dest, tag, comm);
 }
 
 static __device__ int start_send(const void* buf, int count, MPI_Datatype datatype, int dest,
@@ -425,7 +458,9 @@ __device__ int MPI_Irecv(void* buf, int count, MPI_Datatype datatype, int source
         BlockCtx& b = bctx();
         u64 bytes;
         SmallComm sc;
-        if (b.lazy_n < LAZY_MAX && small_call(b, comm, count, datatype, &bytes, &sc) &&
+        int k = b.lazy_n < LAZY_MAX ? small_call(b, comm, count, datatype, &bytes, &sc) : 0;
+        if (k == SMALL_UNCACHED) k = small_comm_cache(comm) ? small_call(b, comm, count, datatype, &bytes, &sc) : 0;
+        if (k == 1 &&
             (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
             (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
@@ -659,26 +694,17 @@ __device__ int MPI_Request_free(MPI_Request* request) {
 
 __device__ int MPI_Send(const void* buf, int count, MPI_Datatype datatype, int dest, int tag,
                         MPI_Comm comm) {
-    {
-        BlockCtx& b = bctx();
-        u64 bytes;
-        SmallComm sc;
-        if (small_call(b, comm, count, datatype, &bytes, &sc) && dest >= 0 && dest < sc.size && tag >= 0 &&
-            tag <= MPI_TAG_UB) {
-            if (api_abort_check(b)) return aborted_code();
-            int rc = MPI_SUCCESS;
-            const int dj = sc.job_rank(dest);
-            // the blocking rendezvous waits without progressing lazy receives:
-            // with some pending, MPI_Wait on an MPI_Isend request waits instead
-            if (bytes <= b.eager_bytes ? leader_send(buf, bytes, dj, sc.ctx, sc.me, tag, &rc)
-                                       : b.lazy_n == 0 && p2p_send_rdv_small(buf, bytes, dj, sc.ctx, sc.me, tag, &rc))
-                return rc;
-        }
+    BlockCtx& b = bctx();
+    u64 bytes;
+    SmallComm sc;
+    const int k = small_call(b, comm, count, datatype, &bytes, &sc);
+    if (k == SMALL_UNCACHED) return send_uncached(buf, count, datatype, dest, tag, comm);
+    if (k && dest >= 0 && dest < sc.size && tag >= 0 && tag <= MPI_TAG_UB) {
+        if (api_abort_check(b)) return aborted_code();
+        const int rc = leader_send(buf, bytes, sc.job_rank(dest), sc.ctx, sc.me, tag);
+        if (rc != LEADER_PASS) return rc;
     }
-    MPI_Request r = MPI_REQUEST_NULL;
-    int rc = MPI_Isend(buf, count, datatype, dest, tag, comm, &r);
-    if (rc) return rc;
-    return MPI_Wait(&r, MPI_STATUS_IGNORE);
+    return send_request_path(buf, count, datatype, dest, tag, comm);
 }
 
 __device__ int MPI_Ssend(const void* buf, int count, MPI_Datatype datatype, int dest, int tag,
@@ -686,24 +712,34 @@ __device__ int MPI_Ssend(const void* buf, int count, MPI_Datatype datatype, int 
     return MPI_Send(buf, count, datatype, dest, tag, comm);
 }
 
-__device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source, int tag,
-                        MPI_Comm comm, MPI_Status* status) {
-    {
-        BlockCtx& b = bctx();
-        u64 bytes;
-        SmallComm sc;
-        if (b.lazy_n == 0 && small_call(b, comm, count, datatype, &bytes, &sc) &&
-            (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
-            (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
-            if (api_abort_check(b)) return aborted_code();
-            int rc = MPI_SUCCESS;
-            if (recv_small(buf, bytes, sc.ctx, source, tag, status, &rc)) return rc;
-        }
-    }
+static __device__ __noinline__ int recv_request_path(void* buf, int count, MPI_Datatype datatype, int source,
+                                                     int tag, MPI_Comm comm, MPI_Status* status) {
     MPI_Request r = MPI_REQUEST_NULL;
     int rc = start_recv(buf, count, datatype, source, tag, comm, &r, /*try_fast=*/true);
     if (rc) return rc;
     return MPI_Wait(&r, status);
+}
+
+static __device__ __noinline__ int recv_uncached(void* buf, int count, MPI_Datatype datatype, int source, int tag,
+                                                 MPI_Comm comm, MPI_Status* status) {
+    if (!small_comm_cache(comm)) return recv_request_path(buf, count, datatype, source, tag, comm, status);
+    return MPI_Recv(buf, count, datatype, source, tag, comm, status);
+}
+
+__device__ int MPI_Recv(void* buf, int count, MPI_Datatype datatype, int source, int tag,
+                        MPI_Comm comm, MPI_Status* status) {
+    BlockCtx& b = bctx();
+    u64 bytes;
+    SmallComm sc;
+    const int k = b.lazy_n == 0 ? small_call(b, comm, count, datatype, &bytes, &sc) : 0;
+    if (k == SMALL_UNCACHED) return recv_uncached(buf, count, datatype, source, tag, comm, status);
+    if (k && (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
+        (tag == MPI_ANY_TAG || (tag >= 0 && tag <= MPI_TAG_UB))) {
+        if (api_abort_check(b)) return aborted_code();
+        const int rc = recv_small(buf, bytes, sc.ctx, source, tag, status);
+        if (rc != LEADER_PASS) return rc;
+    }
+    return recv_request_path(buf, count, datatype, source, tag, comm, status);
 }
 
 // A real exchange; the reference's version was an empty stub (gpu_libs/gpu_mpi/mpi.cu:255-260).
@@ -716,17 +752,16 @@ __device__ int MPI_Sendrecv(const void* sendbuf, int sendcount, MPI_Datatype sen
         BlockCtx& b = bctx();
         u64 sbytes;
         SmallComm sc;
-        if (small_call(b, comm, sendcount, sendtype, &sbytes, &sc) && sbytes <= b.eager_bytes &&
+        int k = small_call(b, comm, sendcount, sendtype, &sbytes, &sc);
+        if (k == SMALL_UNCACHED) k = small_comm_cache(comm) ? small_call(b, comm, sendcount, sendtype, &sbytes, &sc) : 0;
+        if (k == 1 && sbytes <= b.eager_bytes &&
             recvcount >= 0 && (int)recvtype >= 0 && (int)recvtype < GPUMPI_NUM_BASIC_TYPES && dest >= 0 &&
             dest < sc.size && sendtag >= 0 && sendtag <= MPI_TAG_UB &&
             (source == MPI_ANY_SOURCE || (source >= 0 && source < sc.size)) &&
             (recvtag == MPI_ANY_TAG || (recvtag >= 0 && recvtag <= MPI_TAG_UB))) {
             if (api_abort_check(b)) return aborted_code();
-            int rc = MPI_SUCCESS;
-            if (leader_send(sendbuf, sbytes, sc.job_rank(dest), sc.ctx, sc.me, sendtag, &rc)) {
-                if (rc) return rc;
-                return MPI_Recv(recvbuf, recvcount, recvtype, source, recvtag, comm, status);
-            }
+            const int rc = leader_send(sendbuf, sbytes, sc.job_rank(dest), sc.ctx, sc.me, sendtag);
+            if (rc != LEADER_PASS) return rc ? rc : MPI_Recv(recvbuf, recvcount, recvtype, source, recvtag, comm, status);
         }
     }
     MPI_Request rr = MPI_REQUEST_NULL, sr = MPI_REQUEST_NULL;

@@ -688,16 +688,22 @@ __device__ int p2p_small_take(Mailbox* mb, const SmallMatch& m, void* buf, u64 b
     return 1;
 }
 
-// Payloads of at most INLINE_BYTES that are not one aligned access.
-__device__ ulonglong2 tiny_load_bytes(const void* buf, u32 n) {
-    ulonglong2 w = make_ulonglong2(0ull, 0ull);
-    unsigned char* t = reinterpret_cast<unsigned char*>(&w);
-    for (u32 i = 0; i < n && i < INLINE_BYTES; i++) t[i] = ((const unsigned char*)buf)[i];
-    return w;
-}
-__device__ void tiny_store_bytes(void* buf, ulonglong2 w, u32 n) {
-    const unsigned char* t = reinterpret_cast<const unsigned char*>(&w);
-    for (u32 i = 0; i < n && i < INLINE_BYTES; i++) ((unsigned char*)buf)[i] = t[i];
+__device__ int p2p_small_take_st(int slot, int kind, u64 msg_bytes, int src, int tag, void* buf, u64 bytes,
+                                 MPI_Status* st) {
+    BlockCtx& b = bctx();
+    Mailbox* mb = mbox_of(b.rank);
+    SmallMatch m;
+    m.slot = slot;
+    m.src = src;
+    m.tag = tag;
+    m.kind = kind;
+    m.bytes = msg_bytes;
+    m.pre = make_ulonglong2(0ull, 0ull);   // not read: the message is not an inline one
+    int rc = MPI_SUCCESS;
+    u64 got = 0;
+    if (!p2p_small_take(mb, m, buf, bytes, &rc, &got)) return LEADER_PASS;
+    set_status(st, src, tag, rc, got);
+    return rc;
 }
 
 // ---------------------------------------------------------------- lazy receives

@@ -10,6 +10,10 @@
 
 namespace gm {
 
+// Result of a leader-path function that leaves the call to the request path
+// (no MPI return code has this value).
+constexpr int LEADER_PASS = (int)0x80000000;
+
 // ---------------------------------------------------------------- slot claim
 // Leader: claim a free slot of mailbox mb (first guess from the bits last seen
 // there), or -1 when it is full.  The claim is an acquire: the slot is written
@@ -35,24 +39,38 @@ static __device__ __forceinline__ int claim_slot_small(Mailbox* mb) {
 }
 
 // ---------------------------------------------------------------- payloads in the header
-// Up to INLINE_BYTES of payload as two words; aligned 4, 8 and 16-byte
-// payloads are one access, anything else goes byte by byte (p2p.cu).
-__device__ ulonglong2 tiny_load_bytes(const void* buf, u32 n);
-__device__ void tiny_store_bytes(void* buf, ulonglong2 w, u32 n);
-
+// Up to INLINE_BYTES of payload as two little-endian words.  Aligned 4, 8 and
+// 16-byte payloads are one access; other sizes are assembled byte by byte in
+// registers.  No call: a call on this path would make the caller keep its
+// live values in callee-saved registers, saved and restored through local
+// memory on every MPI_Send and MPI_Recv.
 __device__ __forceinline__ ulonglong2 tiny_load(const void* buf, u32 n) {
     const uintptr_t a = (uintptr_t)buf;
     if (n == 8 && (a & 7) == 0) return make_ulonglong2(*(const u64*)buf, 0ull);
     if (n == 4 && (a & 3) == 0) return make_ulonglong2((u64)*(const u32*)buf, 0ull);
     if (n == 16 && (a & 15) == 0) return *(const ulonglong2*)buf;
-    return tiny_load_bytes(buf, n);
+    u64 lo = 0, hi = 0;
+    const unsigned char* p = (const unsigned char*)buf;
+    for (u32 i = 0; i < n && i < INLINE_BYTES; i++) {
+        const u64 v = p[i];
+        if (i < 8) lo |= v << (8 * i);
+        else hi |= v << (8 * (i - 8));
+    }
+    return make_ulonglong2(lo, hi);
 }
 __device__ __forceinline__ void tiny_store(void* buf, ulonglong2 w, u32 n) {
     const uintptr_t a = (uintptr_t)buf;
-    if (n == 8 && (a & 7) == 0) *(u64*)buf = w.x;
-    else if (n == 4 && (a & 3) == 0) *(u32*)buf = (u32)w.x;
-    else if (n == 16 && (a & 15) == 0) *(ulonglong2*)buf = w;
-    else if (n) tiny_store_bytes(buf, w, n);
+    if (n == 8 && (a & 7) == 0) {
+        *(u64*)buf = w.x;
+    } else if (n == 4 && (a & 3) == 0) {
+        *(u32*)buf = (u32)w.x;
+    } else if (n == 16 && (a & 15) == 0) {
+        *(ulonglong2*)buf = w;
+    } else {
+        unsigned char* p = (unsigned char*)buf;
+        for (u32 i = 0; i < n && i < INLINE_BYTES; i++)
+            p[i] = (unsigned char)(i < 8 ? w.x >> (8 * i) : w.y >> (8 * (i - 8)));
+    }
 }
 
 // Leader: blocking send of an eager message of at most INLINE_BYTES, the
@@ -112,15 +130,30 @@ static __device__ __forceinline__ bool small_match(Mailbox* mb, u64 ready, int c
 
 // Receive matched message m of this rank's mailbox into buf (capacity
 // `bytes`): 1 when done (*rc and *got set), 0 when the request path must take
-// it (nothing consumed).  Messages larger than INLINE_BYTES (p2p.cu).
+// it (nothing consumed).  (p2p.cu)
 __device__ int p2p_small_take(Mailbox* mb, const SmallMatch& m, void* buf, u64 bytes, int* rc, u64* got);
+// The same for the message in `slot` of this rank's mailbox, with the status
+// filled in: the MPI result, or LEADER_PASS when the request path must take it.  The
+// match is passed by value so that the inline path keeps it in registers.
+__device__ int p2p_small_take_st(int slot, int kind, u64 msg_bytes, int src, int tag, void* buf, u64 bytes,
+                                 MPI_Status* st);
+
+__device__ __forceinline__ void set_status(MPI_Status* st, int src, int tag, int err, u64 got) {
+    if (st) {
+        st->MPI_SOURCE = src;
+        st->MPI_TAG = tag;
+        st->MPI_ERROR = err;
+        st->gpumpi_count_lo = (int)(got & 0xffffffffu);
+        st->gpumpi_count_hi = (int)(got >> 32);
+    }
+}
 
 // Leader: blocking receive without a request object.  A message of at most
 // INLINE_BYTES is taken here from the registers its header was read into;
-// anything larger goes to p2p_small_take.  Returns 1 (done, or failed: *rc),
-// or 0 when the request path must take the message.
-static __device__ __forceinline__ int recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st,
-                                                 int* rc) {
+// anything larger goes to p2p_small_take_st.  Returns the MPI result (of the
+// receive, or of a failed job), or LEADER_PASS when the request path must take
+// the message.
+static __device__ __forceinline__ int recv_small(void* buf, u64 bytes, int ctx, int source, int tag, MPI_Status* st) {
     BlockCtx& b = bctx();
     Job* j = b.job;
     Mailbox* mb = mbox_of(b.rank);
@@ -131,36 +164,23 @@ static __device__ __forceinline__ int recv_small(void* buf, u64 bytes, int ctx, 
         const u64 ready = mb_ld_acquire(&mb->ready);
         SmallMatch m;
         if (ready && small_match(mb, ready, ctx, source, tag, &m)) {
-            u64 got;
-            if (m.kind == 0 && m.bytes <= INLINE_BYTES) {
-                got = m.bytes < bytes ? m.bytes : bytes;
-                mb_take(mb, m.slot);
-                tiny_store(buf, m.pre, (u32)got);
-                *rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
-            } else if (!p2p_small_take(mb, m, buf, bytes, rc, &got)) {
-                return 0;
-            }
-            if (st) {
-                st->MPI_SOURCE = m.src;
-                st->MPI_TAG = m.tag;
-                st->MPI_ERROR = *rc;
-                st->gpumpi_count_lo = (int)(got & 0xffffffffu);
-                st->gpumpi_count_hi = (int)(got >> 32);
-            }
-            return 1;
+            if (m.kind != 0 || m.bytes > INLINE_BYTES)
+                return p2p_small_take_st(m.slot, m.kind, m.bytes, m.src, m.tag, buf, bytes, st);
+            const u64 got = m.bytes < bytes ? m.bytes : bytes;
+            mb_take(mb, m.slot);
+            tiny_store(buf, m.pre, (u32)got);
+            const int rc = m.bytes > bytes ? MPI_ERR_TRUNCATE : MPI_SUCCESS;
+            set_status(st, m.src, m.tag, rc, got);
+            return rc;
         }
         mb_release_taken();
         // the abort word and the clock every 8th poll: a poll of a mailbox in
         // shared memory is much shorter than a load of the abort word
         if ((it & 7u) == 7u) {
-            if (ld_relaxed_int(&j->status[0]) != 0) {
-                *rc = fail_code(j);
-                return 1;
-            }
+            if (ld_relaxed_int(&j->status[0]) != 0) return fail_code(j);
             if (gtime() - t0 > b.timeout_ns) {
                 job_fail(j, b.rank, GPUMPI_ERR_TIMEOUT, "point-to-point wait timed out");
-                *rc = GPUMPI_ERR_TIMEOUT;
-                return 1;
+                return GPUMPI_ERR_TIMEOUT;
             }
         }
         // the first polls follow each other at once (a reply usually comes
