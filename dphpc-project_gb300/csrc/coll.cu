@@ -644,17 +644,35 @@ static __device__ bool alltoall_flat(const CollArgs& a, const Pub* pub, int P, i
     const u64 nv = b / 16, total = (u64)P * nv;
     uint4* out = reinterpret_cast<uint4*>(a.rbuf);
     constexpr int U = 8;
+    // vector k = q * nv + v of the output comes from vector v of peer q's block;
+    // (q, v) advance by the quotient and remainder of the stride instead of a
+    // 64-bit division per vector
+    const u64 sq = (u64)T / nv, sv = (u64)T % nv;
+    const u64 bq = (u64)U * T / nv, bv = (u64)U * T % nv;
+    u64 q0 = (u64)tid / nv, v0 = (u64)tid % nv;
     for (u64 k0 = (u64)tid; k0 < total; k0 += (u64)U * T) {
         uint4 v[U];
+        u64 q = q0, w = v0;
 #pragma unroll
         for (int u = 0; u < U; u++) {
-            const u64 k = k0 + (u64)u * T;
-            if (k < total) v[u] = __ldcg(reinterpret_cast<const uint4*>(tab[k / nv]) + k % nv);
+            if (q < (u64)P) v[u] = __ldcg(reinterpret_cast<const uint4*>(tab[q]) + w);
+            q += sq;
+            w += sv;
+            if (w >= nv) {
+                w -= nv;
+                q++;
+            }
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const u64 k = k0 + (u64)u * T;
             if (k < total) out[k] = v[u];
+        }
+        q0 += bq;
+        v0 += bv;
+        if (v0 >= nv) {
+            v0 -= nv;
+            q0++;
         }
     }
     bsync();

@@ -94,6 +94,9 @@ __device__ int wait_flags_ge(const u64* flags, int n, u64 target, int skip, int 
 }
 
 // ---------------------------------------------------------------- copies
+// Each thread copies vectors tid, tid + T, ... with U loads in flight, the last
+// partial batch included: a copy of a few vectors per thread (a 2-KiB block
+// copied by one warp) then waits one memory round trip, not one per vector.
 template <class V, int U>
 static __device__ __forceinline__ void copy_vec(V* __restrict__ d, const V* __restrict__ s, u64 nv,
                                                 u64 tid, u64 T) {
@@ -105,7 +108,15 @@ static __device__ __forceinline__ void copy_vec(V* __restrict__ d, const V* __re
 #pragma unroll
         for (int k = 0; k < U; k++) d[i + k * T] = r[k];
     }
-    for (; i < nv; i += T) d[i] = __ldcg(s + i);
+    if (i < nv) {
+        V r[U];
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (i + k * T < nv) r[k] = __ldcg(s + i + k * T);
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (i + k * T < nv) d[i + k * T] = r[k];
+    }
 }
 
 static __device__ __forceinline__ void copy_range(char* d, const char* s, u64 n, u64 tid, u64 T) {

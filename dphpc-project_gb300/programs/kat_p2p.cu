@@ -524,6 +524,50 @@ __device__ int posted_order(int rank, int size) {
     return ok;
 }
 
+// Streams of tiny blocking messages (1..16 bytes, odd buffer offsets) from
+// every other rank to rank 0, more than a mailbox holds, received with
+// MPI_ANY_SOURCE / MPI_ANY_TAG: per sender in send order, with the right
+// size, tag and bytes.
+__device__ unsigned char tiny_byte(int src, int k, int j) { return (unsigned char)((src * 31 + k * 7 + j * 13) & 0xff); }
+__device__ int tiny_len(int src, int k) { return 1 + (k * 7 + src) % 16; }
+
+__device__ int tiny_stream(int rank, int size) {
+    const int n = 200;
+    int ok = 1;
+    unsigned char buf[40];
+    if (rank > 0) {
+        for (int k = 0; k < n; k++) {
+            unsigned char* p = buf + 1 + k % 3;
+            const int len = tiny_len(rank, k);
+            for (int j = 0; j < len; j++) p[j] = tiny_byte(rank, k, j);
+            if (MPI_Send(p, len, MPI_BYTE, 0, k % 4, MPI_COMM_WORLD) != MPI_SUCCESS) ok = 0;
+        }
+    } else {
+        int next[64];
+        for (int r = 0; r < size && r < 64; r++) next[r] = 0;
+        for (int m = 0; m < n * (size - 1); m++) {
+            unsigned char* p = buf + 3 + m % 5;
+            MPI_Status st;
+            if (MPI_Recv(p, 16, MPI_BYTE, MPI_ANY_SOURCE, MPI_ANY_TAG, MPI_COMM_WORLD, &st) != MPI_SUCCESS) ok = 0;
+            const int src = st.MPI_SOURCE;
+            if (src < 1 || src >= size || src >= 64) {
+                ok = 0;
+                continue;
+            }
+            const int k = next[src]++;
+            int cnt = -1;
+            MPI_Get_count(&st, MPI_BYTE, &cnt);
+            if (cnt != tiny_len(src, k) || st.MPI_TAG != k % 4) ok = 0;
+            for (int j = 0; j < cnt && j < 16; j++)
+                if (p[j] != tiny_byte(src, k, j)) ok = 0;
+        }
+        for (int r = 1; r < size && r < 64; r++)
+            if (next[r] != n) ok = 0;
+    }
+    MPI_Barrier(MPI_COMM_WORLD);
+    return ok;
+}
+
 __device__ int __gpu_main(int argc, char** argv) {
     int rank, size, ok = 0;
     MPI_Init(&argc, &argv);
@@ -545,6 +589,7 @@ __device__ int __gpu_main(int argc, char** argv) {
     else if (!strcmp(s, "self_comm")) ok = self_comm(rank, size);
     else if (!strcmp(s, "split_p2p")) ok = split_p2p(rank, size);
     else if (!strcmp(s, "posted_order")) ok = posted_order(rank, size);
+    else if (!strcmp(s, "tiny_stream")) ok = tiny_stream(rank, size);
     printf("%s rank %d ok %d\n", s, rank, ok);
     MPI_Finalize();
     return 0;

@@ -22,6 +22,8 @@ KAT_CASES = [
     ("kat_p2p", "split_p2p", 9),
     ("kat_p2p", "posted_order", 2),
     ("kat_p2p", "posted_order", 3),
+    ("kat_p2p", "tiny_stream", 2),
+    ("kat_p2p", "tiny_stream", 5),
     ("kat_coll", "reduce_prod", 5),
     ("kat_coll", "allreduce_sum", 7),
     ("kat_coll", "allgather", 7),

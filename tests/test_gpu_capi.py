@@ -112,6 +112,69 @@ def test_capi_collectives(coll, form, nranks, count, algo):
     comm.close()
 
 
+@pytest.mark.parametrize("algo", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("per", [3, 17, 250, 333, 4097, 70001])
+def test_capi_misaligned_byte_copies(coll, per, algo):
+    """Alltoall, Allgather and Bcast of bytes whose buffers start at 16-byte
+    phases that differ by rank, so that the pieces of one call reach every
+    pairing of source and destination alignment (the copy engine then moves
+    the widest units both alignments share, down to single bytes).  Every
+    output byte equals the host's, and the bytes just outside each output stay
+    untouched."""
+    import torch
+
+    mod, lib = coll
+    nranks = 6
+    g = torch.Generator().manual_seed(per * 10 + algo)
+    comm = mod.Comm(lib, nranks)
+    keep, descs = [], []
+    pad = 32
+
+    def alloc(nbytes, off):
+        t = torch.full((nbytes + 2 * pad,), 0xA5, dtype=torch.uint8, device="cuda")
+        return t, t.data_ptr() + pad + off
+
+    sends = [torch.randint(0, 256, (per * nranks,), dtype=torch.uint8, generator=g) for _ in range(nranks)]
+    s_buf = [alloc(per * nranks, (5 * r + 3) % 16) for r in range(nranks)]
+    for (t, ptr), x in zip(s_buf, sends):
+        t[ptr - t.data_ptr():ptr - t.data_ptr() + x.numel()] = x.cuda()
+    a2a = [alloc(per * nranks, (7 * r + 1) % 16) for r in range(nranks)]
+    descs.append(mod.make_desc(comm, mod.COLL_ALLTOALL, "uint8", per, [p for _, p in s_buf],
+                               [p for _, p in a2a], 0, 0, keep))
+    ag = [alloc(per * nranks, (3 * r + 9) % 16) for r in range(nranks)]
+    descs.append(mod.make_desc(comm, mod.COLL_ALLGATHER, "uint8", per, [p for _, p in s_buf],
+                               [p for _, p in ag], 0, 0, keep))
+    root = 2
+    bc = [alloc(per * nranks, (11 * r + 6) % 16) for r in range(nranks)]
+    t, ptr = bc[root]
+    t[ptr - t.data_ptr():ptr - t.data_ptr() + per * nranks] = sends[root].cuda()
+    descs.append(mod.make_desc(comm, mod.COLL_BCAST, "uint8", per * nranks, None, [p for _, p in bc], 0, root,
+                               keep))
+    for d in descs:
+        d.algo = algo
+    plan = mod.Plan(lib, descs, threads=128, batched=False)
+    plan.launch()
+    torch.cuda.synchronize()
+    assert mod.status(lib) is None
+    host = [x.numpy() for x in sends]
+
+    def body(tp, nbytes):
+        t, ptr = tp
+        a = t.cpu().numpy()
+        o = ptr - t.data_ptr()
+        assert (a[:o] == 0xA5).all() and (a[o + nbytes:] == 0xA5).all(), "bytes outside the output changed"
+        return a[o:o + nbytes]
+
+    for r in range(nranks):
+        exp_a2a = np.concatenate([host[q][r * per:(r + 1) * per] for q in range(nranks)])
+        assert np.array_equal(body(a2a[r], per * nranks), exp_a2a)
+        exp_ag = np.concatenate([host[q][:per] for q in range(nranks)])
+        assert np.array_equal(body(ag[r], per * nranks), exp_ag)
+        assert np.array_equal(body(bc[r], per * nranks), host[root])
+    plan.close()
+    comm.close()
+
+
 def test_capi_batched_many_comms(coll):
     """Sixteen communicators of uneven sizes in one persistent launch."""
     import torch
