@@ -116,7 +116,7 @@ class ClockSampler:
 # from a one-pass ncu capture of dram__bytes_read.sum + dram__bytes_write.sum
 # (profiles/gpumpi_plan_kernel_batched_collectives.md); other per-rank counts
 # scale it by their elements per rank.
-NCU_TRAFFIC_BYTES_2_16 = 1832801280 + 2687147776
+NCU_TRAFFIC_BYTES_2_16 = 1834974208 + 2673922048
 
 
 ALL_KINDS = ("bcast", "allreduce", "alltoall")
@@ -810,7 +810,7 @@ def main():
                          "frac": round(kernel_gbs / peak, 4), "peak_kind": peak_kind,
                          "traffic": int(NCU_TRAFFIC_BYTES_2_16 * n / (1 << 16)) if kinds == ALL_KINDS else None,
                          "traffic_note": ("bytes per launch: ncu DRAM read+write of the same launch at 2^16 "
-                                          "elements per rank (4.52 GB, 1.12x its algorithmic bytes), scaled by "
+                                          "elements per rank (4.51 GB, 1.12x its algorithmic bytes), scaled by "
                                           "elements per rank"),
                          "algorithmic_bytes": int(nbytes)},
             "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),

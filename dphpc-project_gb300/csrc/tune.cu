@@ -197,7 +197,37 @@ extern "C" int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_
             set_last_error("gpumpi_autotune: the batched list fits at no thread count");
             rc = GPUMPI_ENORES;
         }
-        // group refinement at the winning thread count
+        // group refinement at the winning thread count.  Each change is judged
+        // against the configuration it would replace, the two timed in
+        // alternation (the best of PAIRED_ROUNDS each) and adopted only when
+        // faster by more than ADOPT_MARGIN: launches of one configuration
+        // differ by about a percent from run to run, more than some of the
+        // differences between schedules.
+        constexpr int PAIRED_ROUNDS = 3;
+        constexpr double ADOPT_MARGIN = 0.005;
+        auto time_config = [&](const std::vector<int>& algo, const std::vector<int>& sync, double* us) -> int {
+            for (int i = 0; i < ndesc; i++) {
+                work[i].algo = algo[i];
+                work[i].sync = sync[i];
+            }
+            return time_batched(kThreads[best_t], us);
+        };
+        // 1 when (algo, sync) beats the current best; its time in *us
+        auto better = [&](const std::vector<int>& algo, const std::vector<int>& sync, double* us, int* out) -> int {
+            double cand = 1e300, inc = 1e300;
+            for (int r = 0; r < PAIRED_ROUNDS; r++) {
+                double t = 0.0;
+                int trc = time_config(algo, sync, &t);
+                if (trc) return trc;
+                cand = std::min(cand, t);
+                trc = time_config(best_algo, best_sync, &t);
+                if (trc) return trc;
+                inc = std::min(inc, t);
+            }
+            *us = cand;
+            *out = cand < inc * (1.0 - ADOPT_MARGIN);
+            return 0;
+        };
         std::vector<std::pair<int, int>> groups;
         for (int i = 0; i < ndesc && !rc; i++) {
             const std::pair<int, int> g(descs[i].op, descs[i].dtype);
@@ -209,39 +239,38 @@ extern "C" int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_
             };
             const std::vector<int> cands = algos_of(groups[gi].first);
             for (size_t ci = 0; cands.size() >= 2 && ci < cands.size() && !rc; ci++) {
-                for (int i = 0; i < ndesc; i++) {
-                    work[i].algo = in_group(i) ? cands[ci] : best_algo[i];
-                    work[i].sync = best_sync[i];
-                }
+                std::vector<int> algo(best_algo);
+                bool same = true;
+                for (int i = 0; i < ndesc; i++)
+                    if (in_group(i)) {
+                        same = same && algo[i] == cands[ci];
+                        algo[i] = cands[ci];
+                    }
+                if (same) continue;   // the current best already
                 double us = 0.0;
-                rc = time_batched(kThreads[best_t], &us);
+                int adopt = 0;
+                rc = better(algo, best_sync, &us, &adopt);
                 if (rc) break;
                 if (verbose)
-                    fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d algo %d: %.2f us\n", groups[gi].first,
-                            groups[gi].second, cands[ci], us);
-                if (us < best_us) {
-                    best_us = us;
-                    for (int i = 0; i < ndesc; i++) best_algo[i] = work[i].algo;
-                }
+                    fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d algo %d: %.2f us%s\n", groups[gi].first,
+                            groups[gi].second, cands[ci], us, adopt ? " (adopted)" : "");
+                if (adopt) best_algo = algo;
             }
             if (rc) break;
             // the group's calls with flag rounds (a launch-ordered plan leaves its
             // ranks unsynchronised; readers of one buffer that run in step share
             // its lines in L2)
-            for (int i = 0; i < ndesc; i++) {
-                work[i].algo = best_algo[i];
-                work[i].sync = in_group(i) ? 1 : best_sync[i];
-            }
+            std::vector<int> sync(best_sync);
+            for (int i = 0; i < ndesc; i++)
+                if (in_group(i)) sync[i] = 1;
             double us = 0.0;
-            rc = time_batched(kThreads[best_t], &us);
+            int adopt = 0;
+            rc = better(best_algo, sync, &us, &adopt);
             if (rc) break;
             if (verbose)
-                fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d with flag rounds: %.2f us\n",
-                        groups[gi].first, groups[gi].second, us);
-            if (us < best_us) {
-                best_us = us;
-                for (int i = 0; i < ndesc; i++) best_sync[i] = work[i].sync;
-            }
+                fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d with flag rounds: %.2f us%s\n",
+                        groups[gi].first, groups[gi].second, us, adopt ? " (adopted)" : "");
+            if (adopt) best_sync = sync;
         }
         if (!rc) {
             *batched_threads = kThreads[best_t];
