@@ -237,23 +237,34 @@ extern "C" int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_
             auto in_group = [&](int i) {
                 return descs[i].op == groups[gi].first && descs[i].dtype == groups[gi].second;
             };
+            // candidates: one schedule for every call of the group, then, for each
+            // schedule a the group's calls use, those calls moved to schedule b
+            // (the plain form's per-call picks are a mix whose parts the batched
+            // launch ranks differently)
             const std::vector<int> cands = algos_of(groups[gi].first);
-            for (size_t ci = 0; cands.size() >= 2 && ci < cands.size() && !rc; ci++) {
+            std::vector<std::pair<int, int>> moves;   // (from, to); from = -1: every call
+            for (int b : cands) moves.emplace_back(-1, b);
+            for (int a : cands)
+                for (int b : cands)
+                    if (a != b) moves.emplace_back(a, b);
+            for (size_t mi = 0; cands.size() >= 2 && mi < moves.size() && !rc; mi++) {
                 std::vector<int> algo(best_algo);
-                bool same = true;
+                bool changed = false;
                 for (int i = 0; i < ndesc; i++)
-                    if (in_group(i)) {
-                        same = same && algo[i] == cands[ci];
-                        algo[i] = cands[ci];
+                    if (in_group(i) && (moves[mi].first < 0 || algo[i] == moves[mi].first) &&
+                        algo[i] != moves[mi].second) {
+                        algo[i] = moves[mi].second;
+                        changed = true;
                     }
-                if (same) continue;   // the current best already
+                if (!changed) continue;   // nothing to move, or the current best already
                 double us = 0.0;
                 int adopt = 0;
                 rc = better(algo, best_sync, &us, &adopt);
                 if (rc) break;
                 if (verbose)
-                    fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d algo %d: %.2f us%s\n", groups[gi].first,
-                            groups[gi].second, cands[ci], us, adopt ? " (adopted)" : "");
+                    fprintf(stderr, "GPUMPI tune: batched group op %d dtype %d algo %d -> %d: %.2f us%s\n",
+                            groups[gi].first, groups[gi].second, moves[mi].first, moves[mi].second, us,
+                            adopt ? " (adopted)" : "");
                 if (adopt) best_algo = algo;
             }
             if (rc) break;
