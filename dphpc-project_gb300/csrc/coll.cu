@@ -69,10 +69,18 @@ static __device__ __forceinline__ int wait_one(const u64* flags, int q, u64 seq,
     return (int)bcast(rc, tid);
 }
 
+// Elements per rank segment of an n-element reduction over P ranks: a whole
+// number of 16-byte vectors, and of 128-byte lines once a segment is at least
+// SEG_LINE_MIN_BYTES, so that no line of an input or an output is split
+// between two ranks' segments (a line written in two parts at different times
+// can be written back to DRAM twice, and one read in two parts fetched twice).
+constexpr u64 SEG_LINE_MIN_BYTES = 4096;
 static __device__ __forceinline__ u64 seg_len(u64 n, int P, int es) {
     u64 per = (n + P - 1) / P;
-    u64 vec = es < 16 ? 16 / es : 1;
-    per = (per + vec - 1) / vec * vec;
+    const u64 vec = es < 16 ? 16 / es : 1;
+    const u64 line = es < 128 ? 128 / es : 1;
+    const u64 unit = per * (u64)es >= SEG_LINE_MIN_BYTES ? line : vec;
+    per = (per + unit - 1) / unit * unit;
     return per;
 }
 
