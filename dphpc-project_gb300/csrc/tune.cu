@@ -197,7 +197,7 @@ extern "C" int gpumpi_autotune(gpumpi_coll_desc* descs, int ndesc, const gpumpi_
             set_last_error("gpumpi_autotune: the batched list fits at no thread count");
             rc = GPUMPI_ENORES;
         }
-        // group refinement at the winning thread count.  Each change is judged
+        // group refinement at the winning thread count.  Each change is compared
         // against the configuration it would replace, the two timed in
         // alternation (the best of PAIRED_ROUNDS each) and adopted only when
         // faster by more than ADOPT_MARGIN: launches of one configuration
