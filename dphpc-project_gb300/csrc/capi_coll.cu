@@ -612,7 +612,7 @@ extern "C" int gpumpi_plan_launch_ordered(gpumpi_plan_t p) {
 
 extern "C" int gpumpi_plan_capture(gpumpi_plan_t p, void* stream) {
     if (!p) return GPUMPI_EINVAL;
-    cudaStream_t st = (cudaStream_t)stream;
+    (void)stream;   // captured on a private stream; replays go to the stream given to gpumpi_plan_launch
     cudaStream_t cap;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
@@ -626,7 +626,6 @@ extern "C" int gpumpi_plan_capture(gpumpi_plan_t p, void* stream) {
     CK(e);
     CK(cudaGraphInstantiate(&p->exec, g, 0));
     p->graph = g;
-    (void)st;
     return GPUMPI_OK;
 }
 

@@ -244,7 +244,9 @@ int gpumpi_plan_launch(gpumpi_plan_t plan, void* stream);
 int gpumpi_plan_set_sync(gpumpi_plan_t plan, int mode);
 /* 1 when the plan's launches run the launch-ordered forms, else 0. */
 int gpumpi_plan_launch_ordered(gpumpi_plan_t plan);
-/* Capture the plan's launches once as a CUDA graph; later launches replay it. */
+/* Capture the plan's launches once as a CUDA graph; later launches replay it
+ * on the stream given to gpumpi_plan_launch.  `stream` is not used (the
+ * capture runs on a private stream). */
 int gpumpi_plan_capture(gpumpi_plan_t plan, void* stream);
 /* Host-buffer form: per-rank host->device copies of the send data, the plan,
  * device->host copies of the results, all enqueued on one stream.  host_send
