@@ -519,6 +519,7 @@ __device__ bool program_block_begin(const Launch& L) {
     u32 C, crank;
     asm("mov.u32 %0, %%cluster_nctarank;" : "=r"(C));
     asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(crank));
+    const u32 launch_cluster = C;   // blocks in this launch's clusters
     if (L.job_cluster) {
         C = 1;
         crank = 0;
@@ -530,7 +531,11 @@ __device__ bool program_block_begin(const Launch& L) {
             b.job = nullptr;
         } else {
             block_ctx_init(&L.jobs[jid], L.slot_rank[slot], L.slot_base + slot, C, crank);
-            if (L.job_cluster) {
+            // mailboxes in shared memory only when the launch really made the
+            // job's ranks one cluster (the same answer in every block of the
+            // launch); otherwise the ranks keep their mailboxes in HBM, which
+            // every job has, instead of addressing blocks outside their cluster
+            if (L.job_cluster && launch_cluster == (u32)L.jobs[jid].nranks) {
                 extern __shared__ __align__(16) char gm_dsmem[];
                 u32 dyn;
                 asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
@@ -542,7 +547,7 @@ __device__ bool program_block_begin(const Launch& L) {
     __syncthreads();
     if (L.job_cluster) {
         // every block clears its mailbox before any block may write to it
-        if (b.job) blk_memset(b.mb_local, 0, sizeof(Mailbox), (int)threadIdx.x, (int)blockDim.x);
+        if (b.job && b.mb_cluster) blk_memset(b.mb_local, 0, sizeof(Mailbox), (int)threadIdx.x, (int)blockDim.x);
         asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
     }
     if (!b.job) return false;
